@@ -1,0 +1,173 @@
+"""Block linear algebra on torch complex64 CUDA tensors through the C ABI.
+
+Each function mirrors a reference helper of eigenfns/solver.py:
+  gram      :35-43    <A_i, B_j> over the flattened vectors
+  combine   :49-57    out_i = sum_j C[j, i] S_j over concatenated blocks
+  rotate    tensordot(C.T, S, axes=(1, 0)) (:106, :125, :256, :261-262, :274)
+  deflate   :95-110   X <- X - L (L^H X), chunk by chunk
+Vectors are (m, ...) complex64 tensors; results of reductions are complex128 /
+float64 device tensors. Every kernel is the library's; there is no fallback.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from ._lib import call
+
+_WS: dict = {}
+
+
+def _stream():
+    return torch.cuda.current_stream().cuda_stream
+
+
+def workspace(nbytes: int, device, slot: str = "blas") -> torch.Tensor:
+    """A per-device, per-slot scratch buffer that only grows."""
+    key = (str(device), slot)
+    buf = _WS.get(key)
+    if buf is None or buf.numel() < nbytes:
+        buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+        _WS[key] = buf
+    return buf
+
+
+def _c64(x: torch.Tensor) -> torch.Tensor:
+    if not isinstance(x, torch.Tensor):
+        raise TypeError("expected a torch tensor")
+    if x.dtype != torch.complex64 or not x.is_cuda:
+        raise ValueError(f"expected a complex64 CUDA tensor, got {x.dtype} on {x.device}")
+    return x.contiguous()
+
+
+def _rows(x: torch.Tensor):
+    m = int(x.shape[0])
+    K = int(x.numel() // max(m, 1))
+    return m, K
+
+
+def gram(A: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
+    """(ma, mb) complex128 device matrix <A_i, B_j>."""
+    A, B = _c64(A), _c64(B)
+    ma, K = _rows(A)
+    mb, Kb = _rows(B)
+    if K != Kb:
+        raise ValueError("gram: vector sizes differ")
+    out = torch.empty((ma, mb), dtype=torch.complex128, device=A.device)
+    from ._lib import load
+    nbytes = load().ef_gram_workspace_bytes(ma, mb, K)
+    ws = workspace(nbytes, A.device, "gram")
+    call("ef_gram", A.data_ptr(), B.data_ptr(), ma, mb, K, out.data_ptr(), ws.data_ptr(),
+         ws.numel(), _stream())
+    return out
+
+
+def _coef(C, device) -> torch.Tensor:
+    if isinstance(C, torch.Tensor):
+        return C.to(device=device, dtype=torch.complex64).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(C, np.complex64))).to(device)
+
+
+def rotate(C, S: torch.Tensor, out: torch.Tensor | None = None, mode: int = 0) -> torch.Tensor:
+    """out_i (mode 0: =, 1: +=, -1: -=) sum_j C[j, i] S_j for C (m_in, m_out)."""
+    S = _c64(S)
+    m_in, K = _rows(S)
+    Cd = _coef(C, S.device)
+    if Cd.shape[0] != m_in:
+        raise ValueError(f"rotate: C has {Cd.shape[0]} rows for {m_in} vectors")
+    m_out = int(Cd.shape[1])
+    if out is None:
+        if mode != 0:
+            raise ValueError("rotate: accumulate modes need an output")
+        out = torch.empty((m_out,) + tuple(S.shape[1:]), dtype=torch.complex64, device=S.device)
+    call("ef_rotate", Cd.data_ptr(), S.data_ptr(), out.data_ptr(), m_in, m_out, K, mode, _stream())
+    return out
+
+
+def combine(C, *blocks: torch.Tensor) -> torch.Tensor:
+    Cd = _coef(C, blocks[0].device)
+    out = None
+    off = 0
+    for Bk in blocks:
+        n = int(Bk.shape[0])
+        piece = Cd[off:off + n].contiguous()
+        out = rotate(piece, Bk, out, 0 if out is None else 1)
+        off += n
+    return out
+
+
+def rowdot(A: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
+    """complex128 (m,) <A_i, B_i>."""
+    A, B = _c64(A), _c64(B)
+    m, K = _rows(A)
+    out = torch.empty((m,), dtype=torch.complex128, device=A.device)
+    from ._lib import load
+    nbytes = load().ef_rowdot_workspace_bytes(m, K)
+    ws = workspace(nbytes, A.device, "rowdot")
+    call("ef_rowdot", A.data_ptr(), B.data_ptr(), m, K, out.data_ptr(), ws.data_ptr(), ws.numel(),
+         _stream())
+    return out
+
+
+def rowstats(A: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
+    """float64 (m, 4): Re<A_i,B_i>, Im<A_i,B_i>, |A_i|^2, |B_i|^2 in one pass."""
+    A, B = _c64(A), _c64(B)
+    m, K = _rows(A)
+    out = torch.empty((m, 4), dtype=torch.float64, device=A.device)
+    from ._lib import load
+    nbytes = load().ef_rowdot_workspace_bytes(m, K)
+    ws = workspace(nbytes, A.device, "rowdot")
+    call("ef_rowstats", A.data_ptr(), B.data_ptr(), m, K, out.data_ptr(), ws.data_ptr(), ws.numel(),
+         _stream())
+    return out
+
+
+def row_norms(X: torch.Tensor) -> torch.Tensor:
+    return torch.sqrt(torch.clamp(rowdot(X, X).real, min=0.0))
+
+
+def residual(HX: torch.Tensor, X: torch.Tensor, lam: torch.Tensor, out: torch.Tensor | None = None):
+    HX, X = _c64(HX), _c64(X)
+    m, K = _rows(X)
+    lam = lam.to(device=X.device, dtype=torch.float64).contiguous()
+    if out is None:
+        out = torch.empty_like(X)
+    call("ef_residual", HX.data_ptr(), X.data_ptr(), lam.data_ptr(), out.data_ptr(), m, K, _stream())
+    return out
+
+
+def scale_rows(X: torch.Tensor, scale: torch.Tensor) -> torch.Tensor:
+    """In place X_i *= scale[i]."""
+    m, K = _rows(X)
+    if not X.is_contiguous():
+        raise ValueError("scale_rows needs a contiguous tensor")
+    scale = scale.to(device=X.device, dtype=torch.float64).contiguous()
+    call("ef_scale_rows", X.data_ptr(), scale.data_ptr(), m, K, _stream())
+    return X
+
+
+def axpby(X: torch.Tensor, Y: torch.Tensor, a: float, b: float) -> torch.Tensor:
+    """In place Y = a X + b Y."""
+    X = _c64(X)
+    if not Y.is_contiguous() or Y.dtype != torch.complex64:
+        raise ValueError("axpby needs a contiguous complex64 output")
+    call("ef_axpby", X.data_ptr(), Y.data_ptr(), int(X.numel()), float(a), float(b), _stream())
+    return Y
+
+
+def deflate(X: torch.Tensor, locked: torch.Tensor | None, chunk_rows: int | None = None) -> torch.Tensor:
+    """X <- X - L (L^H X) over chunks of the locked set (solver.py:95-110), in place.
+
+    `chunk_rows=None` projects against the whole locked set at once (two passes over
+    it); the reference chunks only to cap a 12 GB card's transient memory."""
+    if locked is None or int(locked.shape[0]) == 0:
+        return X
+    if not X.is_contiguous():
+        raise ValueError("deflate works in place on a contiguous block")
+    n = int(locked.shape[0])
+    chunk_rows = n if chunk_rows is None else chunk_rows
+    for s in range(0, n, chunk_rows):
+        chunk = locked[s:s + chunk_rows]
+        Cm = gram(chunk, X).to(torch.complex64)
+        rotate(Cm, chunk, X, -1)
+    return X

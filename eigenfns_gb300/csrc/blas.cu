@@ -1,0 +1,607 @@
+// Block linear algebra on complex64 vector blocks.
+//
+// Reference: eigenfns/solver.py -- gram (:35-43, true-fp32 X^H Y), combine and
+// the tensordot rotations (:49-57, :106, :125, :256, :261-262, :274), row norms and
+// Rayleigh quotients (:228-238), residual R = HX - lam X (:229), random start
+// blocks (:196-205); eigenfns/chebyshev.py:248 and scripts/exp/exp_kpm_dos.py:139-140
+// (Rademacher probes).
+//
+// Gram: each CTA owns a 32x32 output tile and one K-chunk (split-K). Products and
+// short runs of sums are fp32 on the CUDA cores; every 256 k-values the fp32 run
+// is flushed into an fp64 accumulator, and the chunks are reduced in fp64 in a
+// fixed order, so results are deterministic and the long sums keep fp64 accuracy.
+#include <cstdint>
+#include <cstring>
+
+#include "common.cuh"
+#include "dft.cuh"
+#include "status.h"
+
+using namespace ef;
+
+namespace {
+
+constexpr int GT = 32;      // gram output tile edge
+constexpr int GBK = 32;     // k-values per shared-memory stage
+constexpr int GFLUSH = 8;   // stages per fp64 flush (256 k-values)
+constexpr int GTHREADS = 64;
+
+__global__ void __launch_bounds__(GTHREADS) gram_kernel(const float2* __restrict__ A,
+                                                        const float2* __restrict__ B, int ma, int mb,
+                                                        long long K, long long kchunk,
+                                                        double2* __restrict__ partial) {
+  __shared__ float2 As[GBK][GT + 1];
+  __shared__ float2 Bs[GBK][GT + 1];
+  const int tid = threadIdx.x;
+  const int ti = tid & 7, tj = tid >> 3;
+  const int i0 = blockIdx.x * GT, j0 = blockIdx.y * GT;
+  const long long kbeg = (long long)blockIdx.z * kchunk;
+  long long kend = kbeg + kchunk;
+  if (kend > K) kend = K;
+  float accr[4][4], acci[4][4];
+  double dr[4][4], di[4][4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) { accr[r][c] = acci[r][c] = 0.f; dr[r][c] = di[r][c] = 0.0; }
+  int stage = 0;
+  for (long long k0 = kbeg; k0 < kend; k0 += GBK) {
+    // cooperative load of a 32 x 32 tile of A and of B (row, k), transposed into smem
+#pragma unroll
+    for (int l = 0; l < (GT * GBK) / GTHREADS; ++l) {
+      int e = tid + l * GTHREADS;
+      int row = e / GBK, kk = e % GBK;
+      long long k = k0 + kk;
+      float2 va = make_float2(0.f, 0.f), vb = make_float2(0.f, 0.f);
+      if (k < kend) {
+        if (i0 + row < ma) va = A[(long long)(i0 + row) * K + k];
+        if (j0 + row < mb) vb = B[(long long)(j0 + row) * K + k];
+      }
+      As[kk][row] = va;
+      Bs[kk][row] = vb;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < GBK; ++kk) {
+      float2 a[4], b[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) a[r] = As[kk][ti + 8 * r];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) b[c] = Bs[kk][tj + 8 * c];
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          // conj(a) * b
+          accr[r][c] = fmaf(a[r].x, b[c].x, fmaf(a[r].y, b[c].y, accr[r][c]));
+          acci[r][c] = fmaf(a[r].x, b[c].y, fmaf(-a[r].y, b[c].x, acci[r][c]));
+        }
+    }
+    __syncthreads();
+    if (++stage == GFLUSH) {
+      stage = 0;
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          dr[r][c] += (double)accr[r][c];
+          di[r][c] += (double)acci[r][c];
+          accr[r][c] = acci[r][c] = 0.f;
+        }
+    }
+  }
+  double2* out = partial + (long long)blockIdx.z * ma * mb;
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      int i = i0 + ti + 8 * r, j = j0 + tj + 8 * c;
+      if (i < ma && j < mb)
+        out[(long long)i * mb + j] = make_double2(dr[r][c] + (double)accr[r][c], di[r][c] + (double)acci[r][c]);
+    }
+}
+
+// Pipelined variant for 16-byte aligned rows of even length: 128 threads own a 32x32
+// tile (2 x 4 outputs each), tiles of A and B rows stream through two shared-memory
+// stages with cp.async while the previous stage is multiplied. fp32 inside the CTA's
+// K-chunk, fp64 across chunks.
+constexpr int PG_THREADS = 128;
+constexpr int PG_BK = 32;                 // complex k-values per stage
+constexpr int PG_LD = PG_BK + 2;          // row stride in float2 (272 B, 16-byte aligned)
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, int src_bytes) {
+  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+__global__ void __launch_bounds__(PG_THREADS) gram_pipe_kernel(const float2* __restrict__ A,
+                                                               const float2* __restrict__ B, int ma,
+                                                               int mb, long long K, long long kchunk,
+                                                               double2* __restrict__ partial) {
+  __shared__ __align__(16) float2 As[2][GT][PG_LD];
+  __shared__ __align__(16) float2 Bs[2][GT][PG_LD];
+  const int tid = threadIdx.x;
+  const int ti = tid & 15, tj = tid >> 4;   // rows ti, ti+16; cols tj + 8c
+  const int i0 = blockIdx.x * GT, j0 = blockIdx.y * GT;
+  const long long kbeg = (long long)blockIdx.z * kchunk;
+  long long kend = kbeg + kchunk;
+  if (kend > K) kend = K;
+  const int nst = (int)((kend - kbeg + PG_BK - 1) / PG_BK);
+  // each stage: 32 rows x 16 chunks of 16 B for A and for B = 1024 copies, 8 per thread
+  auto issue = [&](int stage, int buf) {
+    const long long k0 = kbeg + (long long)stage * PG_BK;
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+      int e = tid + l * PG_THREADS;      // 0..511
+      int row = e >> 4, ch = e & 15;     // chunk of 2 complex values
+      long long k = k0 + 2 * ch;
+      long long left = kend - k;
+      int bytes = left >= 2 ? 16 : (left == 1 ? 8 : 0);
+      int ra = i0 + row, rb = j0 + row;
+      const float2* ga = A + (long long)(ra < ma ? ra : 0) * K + (bytes ? k : 0);
+      const float2* gb = B + (long long)(rb < mb ? rb : 0) * K + (bytes ? k : 0);
+      cp_async16(&As[buf][row][2 * ch], ga, ra < ma ? bytes : 0);
+      cp_async16(&Bs[buf][row][2 * ch], gb, rb < mb ? bytes : 0);
+    }
+    cp_async_commit();
+  };
+  float accr[2][4], acci[2][4];
+#pragma unroll
+  for (int r = 0; r < 2; ++r)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) accr[r][c] = acci[r][c] = 0.f;
+  if (nst > 0) issue(0, 0);
+  for (int st = 0; st < nst; ++st) {
+    const int buf = st & 1;
+    if (st + 1 < nst) {
+      issue(st + 1, buf ^ 1);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < PG_BK; ++kk) {
+      float2 a0 = As[buf][ti][kk], a1 = As[buf][ti + 16][kk];
+      float2 b[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) b[c] = Bs[buf][tj + 8 * c][kk];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        accr[0][c] = fmaf(a0.x, b[c].x, fmaf(a0.y, b[c].y, accr[0][c]));
+        acci[0][c] = fmaf(a0.x, b[c].y, fmaf(-a0.y, b[c].x, acci[0][c]));
+        accr[1][c] = fmaf(a1.x, b[c].x, fmaf(a1.y, b[c].y, accr[1][c]));
+        acci[1][c] = fmaf(a1.x, b[c].y, fmaf(-a1.y, b[c].x, acci[1][c]));
+      }
+    }
+    __syncthreads();
+  }
+  double2* out = partial + (long long)blockIdx.z * ma * mb;
+#pragma unroll
+  for (int r = 0; r < 2; ++r)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      int i = i0 + ti + 16 * r, j = j0 + tj + 8 * c;
+      if (i < ma && j < mb) out[(long long)i * mb + j] = make_double2((double)accr[r][c], (double)acci[r][c]);
+    }
+}
+
+__global__ void gram_reduce_kernel(const double2* __restrict__ partial, int nsplit, int n,
+                                   double2* __restrict__ G) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  double sr = 0.0, si = 0.0;
+  for (int s = 0; s < nsplit; ++s) {
+    double2 p = partial[(long long)s * n + e];
+    sr += p.x;
+    si += p.y;
+  }
+  G[e] = make_double2(sr, si);
+}
+
+int gram_splits(int ma, int mb, long long K) {
+  long long tiles = (long long)((ma + GT - 1) / GT) * ((mb + GT - 1) / GT);
+  long long target = 4096 / (tiles > 0 ? tiles : 1);
+  long long maxs = (K + 2047) / 2048;   // at least 2048 k-values per chunk
+  long long s = target < maxs ? target : maxs;
+  if (s < 1) s = 1;
+  return (int)s;
+}
+
+// ---- rotation ---------------------------------------------------------------------
+constexpr int RT = 32;      // outputs per thread
+constexpr int RTHREADS = 256;
+
+__global__ void __launch_bounds__(RTHREADS) rotate_kernel(const float2* __restrict__ C,
+                                                          const float2* __restrict__ S,
+                                                          float2* __restrict__ out, int m_in,
+                                                          int m_out, long long K, int mode) {
+  extern __shared__ float2 Cs[];  // (m_in, RT) slice of C for this output tile
+  const int i0 = blockIdx.y * RT;
+  const int nt = (m_out - i0) < RT ? (m_out - i0) : RT;
+  for (int e = threadIdx.x; e < m_in * RT; e += blockDim.x) {
+    int j = e / RT, ii = e % RT;
+    Cs[e] = (ii < nt) ? C[(long long)j * m_out + i0 + ii] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < K;
+       k += (long long)gridDim.x * blockDim.x) {
+    float2 acc[RT];
+#pragma unroll
+    for (int ii = 0; ii < RT; ++ii) acc[ii] = make_float2(0.f, 0.f);
+    for (int j = 0; j < m_in; ++j) {
+      float2 s = S[(long long)j * K + k];
+      const float2* cj = Cs + j * RT;
+#pragma unroll
+      for (int ii = 0; ii < RT; ++ii) {
+        float2 c = cj[ii];
+        acc[ii].x = fmaf(c.x, s.x, fmaf(-c.y, s.y, acc[ii].x));
+        acc[ii].y = fmaf(c.x, s.y, fmaf(c.y, s.x, acc[ii].y));
+      }
+    }
+#pragma unroll
+    for (int ii = 0; ii < RT; ++ii) {
+      if (ii < nt) {
+        float2* o = out + (long long)(i0 + ii) * K + k;
+        if (mode == 0) *o = acc[ii];
+        else if (mode > 0) { float2 v = *o; *o = make_float2(v.x + acc[ii].x, v.y + acc[ii].y); }
+        else { float2 v = *o; *o = make_float2(v.x - acc[ii].x, v.y - acc[ii].y); }
+      }
+    }
+  }
+}
+
+// ---- per-row statistics ----------------------------------------------------------
+// For each row i: <A_i, B_i> (complex), |A_i|^2, |B_i|^2. Products in fp32, runs of
+// 32 float4 loads flushed into fp64, chunks reduced in fp64 in a fixed order.
+constexpr int DTHREADS = 256;
+
+__global__ void __launch_bounds__(DTHREADS) rowstats_kernel(const float4* __restrict__ A,
+                                                            const float4* __restrict__ B,
+                                                            long long K2, long long kchunk,
+                                                            double4* partial) {
+  __shared__ double red[4][DTHREADS / 32];
+  const int row = blockIdx.y;
+  const long long kb = (long long)blockIdx.x * kchunk;
+  long long ke = kb + kchunk;
+  if (ke > K2) ke = K2;
+  const float4* a = A + (long long)row * K2;
+  const float4* b = B + (long long)row * K2;
+  double s[4] = {0.0, 0.0, 0.0, 0.0};
+  float f[4] = {0.f, 0.f, 0.f, 0.f};
+  int cnt = 0;
+  for (long long k = kb + threadIdx.x; k < ke; k += blockDim.x) {
+    float4 x = a[k], y = b[k];
+    // two complex values per float4: (x.x + i x.y), (x.z + i x.w)
+    f[0] = fmaf(x.x, y.x, fmaf(x.y, y.y, fmaf(x.z, y.z, fmaf(x.w, y.w, f[0]))));
+    f[1] = fmaf(x.x, y.y, fmaf(-x.y, y.x, fmaf(x.z, y.w, fmaf(-x.w, y.z, f[1]))));
+    f[2] = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, f[2]))));
+    f[3] = fmaf(y.x, y.x, fmaf(y.y, y.y, fmaf(y.z, y.z, fmaf(y.w, y.w, f[3]))));
+    if (++cnt == 32) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) { s[q] += f[q]; f[q] = 0.f; }
+      cnt = 0;
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    s[q] += f[q];
+    for (int o = 16; o > 0; o >>= 1) s[q] += __shfl_down_sync(0xffffffffu, s[q], o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) red[q][threadIdx.x >> 5] = s[q];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int w = 0; w < DTHREADS / 32; ++w)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) t[q] += red[q][w];
+    partial[(long long)row * gridDim.x + blockIdx.x] = make_double4(t[0], t[1], t[2], t[3]);
+  }
+}
+
+__global__ void rowstats_reduce_kernel(const double4* partial, int nchunk, int m, double4* out) {
+  int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= m) return;
+  double t[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int c = 0; c < nchunk; ++c) {
+    double4 p = partial[(long long)row * nchunk + c];
+    t[0] += p.x; t[1] += p.y; t[2] += p.z; t[3] += p.w;
+  }
+  out[row] = make_double4(t[0], t[1], t[2], t[3]);
+}
+
+// rows of odd complex length fall back to the scalar kernel below
+__global__ void __launch_bounds__(DTHREADS) rowstats_scalar_kernel(const float2* __restrict__ A,
+                                                                   const float2* __restrict__ B,
+                                                                   long long K, long long kchunk,
+                                                                   double4* partial) {
+  __shared__ double red[4][DTHREADS / 32];
+  const int row = blockIdx.y;
+  const long long kb = (long long)blockIdx.x * kchunk;
+  long long ke = kb + kchunk;
+  if (ke > K) ke = K;
+  const float2* a = A + (long long)row * K;
+  const float2* b = B + (long long)row * K;
+  double s[4] = {0.0, 0.0, 0.0, 0.0};
+  for (long long k = kb + threadIdx.x; k < ke; k += blockDim.x) {
+    float2 x = a[k], y = b[k];
+    s[0] += (double)x.x * y.x + (double)x.y * y.y;
+    s[1] += (double)x.x * y.y - (double)x.y * y.x;
+    s[2] += (double)x.x * x.x + (double)x.y * x.y;
+    s[3] += (double)y.x * y.x + (double)y.y * y.y;
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    for (int o = 16; o > 0; o >>= 1) s[q] += __shfl_down_sync(0xffffffffu, s[q], o);
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) red[q][threadIdx.x >> 5] = s[q];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int w = 0; w < DTHREADS / 32; ++w)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) t[q] += red[q][w];
+    partial[(long long)row * gridDim.x + blockIdx.x] = make_double4(t[0], t[1], t[2], t[3]);
+  }
+}
+
+int rowdot_chunks(long long K) {
+  long long c = (K + 65535) / 65536;
+  if (c < 1) c = 1;
+  if (c > 1024) c = 1024;
+  return (int)c;
+}
+
+// ---- elementwise --------------------------------------------------------------------
+__global__ void residual_kernel(const float2* HX, const float2* X, const double* lam, float2* R,
+                                long long K, long long total) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    float l = (float)lam[i / K];
+    float2 h = HX[i], x = X[i];
+    R[i] = make_float2(h.x - l * x.x, h.y - l * x.y);
+  }
+}
+
+__global__ void scale_rows_kernel(float2* X, const double* scale, long long K, long long total) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    float s = (float)scale[i / K];
+    float2 x = X[i];
+    X[i] = make_float2(x.x * s, x.y * s);
+  }
+}
+
+__global__ void axpby_kernel(const float2* X, float2* Y, long long n, float a, float b) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    float2 x = X[i], y = Y[i];
+    Y[i] = make_float2(a * x.x + b * y.x, a * x.y + b * y.y);
+  }
+}
+
+// splitmix64 finaliser; the same words as the oracle's counter generator
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__global__ void rand_kernel(const float* kax, int G, float2* X, long long total, uint64_t key,
+                            int kind) {
+  const long long N = (long long)G * G * G;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    uint64_t w = mix64(key + (uint64_t)(i + 1) * 0x9E3779B97F4A7C15ull);
+    long long vox = i % N;
+    int z = vox % G, y = (vox / G) % G, x = vox / ((long long)G * G);
+    bool live = !(kax[x] == 0.f && kax[G + y] == 0.f && kax[2 * G + z] == 0.f);
+    float2 v;
+    if (kind == EF_RAND_NORMAL) {
+      float u1 = ((float)(w >> 40) + 0.5f) * 5.9604644775390625e-08f;
+      float u2 = ((float)((w >> 16) & 0xFFFFFFull) + 0.5f) * 5.9604644775390625e-08f;
+      float r = sqrtf(-2.0f * logf(u1));
+      float ang = 6.2831855f * u2;
+      float sn, cs;
+      sincosf(ang, &sn, &cs);
+      v = make_float2(r * cs, r * sn);
+    } else {
+      float re = ((w >> 63) & 1ull) ? -1.f : 1.f;
+      if (kind == EF_RAND_RADEMACHER) {
+        v = make_float2(re, 0.f);
+      } else {
+        float im = ((w >> 62) & 1ull) ? -1.f : 1.f;
+        const float h = 0.70710678f;
+        v = make_float2(re * h, im * h);
+      }
+    }
+    X[i] = live ? v : make_float2(0.f, 0.f);
+  }
+}
+
+__global__ void mask_kernel(const float* kax, int G, float2* X, long long total) {
+  const long long N = (long long)G * G * G;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long vox = i % N;
+    int z = vox % G, y = (vox / G) % G, x = vox / ((long long)G * G);
+    if (kax[x] == 0.f && kax[G + y] == 0.f && kax[2 * G + z] == 0.f) X[i] = make_float2(0.f, 0.f);
+  }
+}
+
+int grid_for(long long total) {
+  long long b = (total + 255) / 256;
+  if (b > 152 * 16) b = 152 * 16;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t ef_gram_workspace_bytes(int ma, int mb, long long K) {
+  if (ma <= 0 || mb <= 0 || K <= 0) return 0;
+  return (size_t)gram_splits(ma, mb, K) * ma * mb * sizeof(double2) + 256;
+}
+
+int ef_gram(const float* A, const float* B, int ma, int mb, long long K, double* G, void* work,
+            size_t work_bytes, void* stream) {
+  if (!A || !B || !G || ma <= 0 || mb <= 0 || K <= 0) return ef_fail(EF_ERR_INVALID, "bad gram arguments");
+  if (!work || work_bytes < ef_gram_workspace_bytes(ma, mb, K))
+    return ef_fail(EF_ERR_WORKSPACE, "gram work buffer too small");
+  cudaStream_t st = (cudaStream_t)stream;
+  int ns = gram_splits(ma, mb, K);
+  long long kchunk = (K + ns - 1) / ns;
+  kchunk = (kchunk + GBK - 1) / GBK * GBK;
+  ns = (int)((K + kchunk - 1) / kchunk);
+  dim3 grid((ma + GT - 1) / GT, (mb + GT - 1) / GT, ns);
+  const bool pipe = (K % 2 == 0) && ((((uintptr_t)A) | ((uintptr_t)B)) % 16 == 0);
+  ef_count_launches(1);
+  if (pipe)
+    gram_pipe_kernel<<<grid, PG_THREADS, 0, st>>>((const float2*)A, (const float2*)B, ma, mb, K,
+                                                  kchunk, (double2*)work);
+  else
+    gram_kernel<<<grid, GTHREADS, 0, st>>>((const float2*)A, (const float2*)B, ma, mb, K, kchunk,
+                                          (double2*)work);
+  int n = ma * mb;
+  ef_count_launches(1);
+  gram_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>((const double2*)work, ns, n, (double2*)G);
+  return ef_check_launch();
+}
+
+int ef_rotate(const float* C, const float* S, float* out, int m_in, int m_out, long long K, int mode,
+              void* stream) {
+  if (!C || !S || !out || m_in <= 0 || m_out <= 0 || K <= 0) return ef_fail(EF_ERR_INVALID, "bad rotate arguments");
+  if ((size_t)m_in * RT * sizeof(float2) > 200 * 1024) return ef_fail(EF_ERR_TOO_LARGE, "m_in too large for rotate");
+  int ty = (m_out + RT - 1) / RT;
+  const char* s0 = (const char*)S;
+  const char* s1 = s0 + (size_t)m_in * K * sizeof(float2);
+  const char* o0 = (const char*)out;
+  const char* o1 = o0 + (size_t)m_out * K * sizeof(float2);
+  bool overlap = (o0 < s1) && (s0 < o1);
+  if (overlap && !(o0 == s0 && ty == 1))
+    return ef_fail(EF_ERR_INVALID, "rotate: out may alias S only exactly and with m_out <= 32");
+  cudaStream_t st = (cudaStream_t)stream;
+  size_t smem = (size_t)m_in * RT * sizeof(float2);
+  if (smem > 48 * 1024) cudaFuncSetAttribute(rotate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  long long bx = (K + RTHREADS - 1) / RTHREADS;
+  long long cap = (152 * 8 + ty - 1) / ty;
+  if (bx > cap) bx = cap;
+  ef_count_launches(1);
+  rotate_kernel<<<dim3((unsigned)bx, ty), RTHREADS, smem, st>>>((const float2*)C, (const float2*)S,
+                                                                (float2*)out, m_in, m_out, K, mode);
+  return ef_check_launch();
+}
+
+static size_t rowstats_partial_bytes(int m, long long K) {
+  return (size_t)m * rowdot_chunks(K) * sizeof(double4) + 256;
+}
+
+size_t ef_rowdot_workspace_bytes(int m, long long K) {
+  if (m <= 0 || K <= 0) return 0;
+  return rowstats_partial_bytes(m, K) + (size_t)m * sizeof(double4) + 512;
+}
+
+int ef_rowstats(const float* A, const float* B, int m, long long K, double* out, void* work,
+                size_t work_bytes, void* stream) {
+  if (!A || !B || !out || m <= 0 || K <= 0) return ef_fail(EF_ERR_INVALID, "bad rowstats arguments");
+  if (!work || work_bytes < rowstats_partial_bytes(m, K)) return ef_fail(EF_ERR_WORKSPACE, "rowstats work buffer too small");
+  cudaStream_t st = (cudaStream_t)stream;
+  int nc = rowdot_chunks(K);
+  bool vec = (K % 2 == 0) && (((uintptr_t)A | (uintptr_t)B) % 16 == 0);
+  if (vec) {
+    long long K2 = K / 2;
+    long long kchunk = (K2 + nc - 1) / nc;
+    ef_count_launches(1);
+    rowstats_kernel<<<dim3(nc, m), DTHREADS, 0, st>>>((const float4*)A, (const float4*)B, K2, kchunk,
+                                                     (double4*)work);
+  } else {
+    long long kchunk = (K + nc - 1) / nc;
+    ef_count_launches(1);
+    rowstats_scalar_kernel<<<dim3(nc, m), DTHREADS, 0, st>>>((const float2*)A, (const float2*)B, K,
+                                                            kchunk, (double4*)work);
+  }
+  ef_count_launches(1);
+  rowstats_reduce_kernel<<<(m + 127) / 128, 128, 0, st>>>((const double4*)work, nc, m, (double4*)out);
+  return ef_check_launch();
+}
+
+__global__ void rowdot_pick_kernel(const double4* s, int m, double2* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) out[i] = make_double2(s[i].x, s[i].y);
+}
+
+int ef_rowdot(const float* A, const float* B, int m, long long K, double* out, void* work,
+              size_t work_bytes, void* stream) {
+  if (!A || !B || !out || m <= 0 || K <= 0) return ef_fail(EF_ERR_INVALID, "bad rowdot arguments");
+  if (!work || work_bytes < ef_rowdot_workspace_bytes(m, K)) return ef_fail(EF_ERR_WORKSPACE, "rowdot work buffer too small");
+  size_t pb = (rowstats_partial_bytes(m, K) + 255) / 256 * 256;
+  double4* stats = reinterpret_cast<double4*>(reinterpret_cast<char*>(work) + pb);
+  int r = ef_rowstats(A, B, m, K, (double*)stats, work, pb, stream);
+  if (r != EF_OK) return r;
+  ef_count_launches(1);
+  rowdot_pick_kernel<<<(m + 127) / 128, 128, 0, (cudaStream_t)stream>>>(stats, m, (double2*)out);
+  return ef_check_launch();
+}
+
+int ef_residual(const float* HX, const float* X, const double* lam, float* R, int m, long long K,
+                void* stream) {
+  if (!HX || !X || !lam || !R || m <= 0 || K <= 0) return ef_fail(EF_ERR_INVALID, "bad residual arguments");
+  long long total = (long long)m * K;
+  ef_count_launches(1);
+  residual_kernel<<<grid_for(total), 256, 0, (cudaStream_t)stream>>>((const float2*)HX, (const float2*)X,
+                                                                      lam, (float2*)R, K, total);
+  return ef_check_launch();
+}
+
+int ef_scale_rows(float* X, const double* scale, int m, long long K, void* stream) {
+  if (!X || !scale || m <= 0 || K <= 0) return ef_fail(EF_ERR_INVALID, "bad scale arguments");
+  long long total = (long long)m * K;
+  ef_count_launches(1);
+  scale_rows_kernel<<<grid_for(total), 256, 0, (cudaStream_t)stream>>>((float2*)X, scale, K, total);
+  return ef_check_launch();
+}
+
+int ef_axpby(const float* X, float* Y, long long n_complex, double a, double b, void* stream) {
+  if (!X || !Y || n_complex <= 0) return ef_fail(EF_ERR_INVALID, "bad axpby arguments");
+  ef_count_launches(1);
+  axpby_kernel<<<grid_for(n_complex), 256, 0, (cudaStream_t)stream>>>((const float2*)X, (float2*)Y,
+                                                                       n_complex, (float)a, (float)b);
+  return ef_check_launch();
+}
+
+int ef_rand_block(const ef_op* op, float* X, int m, uint64_t seed, uint64_t stream_id, int kind,
+                  void* stream) {
+  const ef::Op* o = op;
+  if (!o || !X || m <= 0 || kind < 0 || kind > 2) return ef_fail(EF_ERR_INVALID, "bad rand arguments");
+  uint64_t s = seed * 0x9E3779B97F4A7C15ull + stream_id * 0xC2B2AE3D27D4EB4Full + 1ull;
+  // key = mix(seed * phi + stream * c2 + 1), computed on the host like the oracle
+  uint64_t z = s;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  uint64_t key = z ^ (z >> 31);
+  long long total = (long long)m * 2 * o->N;
+  ef_count_launches(1);
+  rand_kernel<<<grid_for(total), 256, 0, (cudaStream_t)stream>>>(o->kax, o->G, (float2*)X, total, key, kind);
+  return ef_check_launch();
+}
+
+int ef_apply_mask(const ef_op* op, float* X, int m, void* stream) {
+  const ef::Op* o = op;
+  if (!o || !X || m <= 0) return ef_fail(EF_ERR_INVALID, "bad mask arguments");
+  long long total = (long long)m * 2 * o->N;
+  ef_count_launches(1);
+  mask_kernel<<<grid_for(total), 256, 0, (cudaStream_t)stream>>>(o->kax, o->G, (float2*)X, total);
+  return ef_check_launch();
+}
+
+}  // extern "C"

@@ -1,0 +1,49 @@
+// Library metadata and status reporting of the C ABI.
+#include <cstdio>
+#include <string>
+
+#include "../../include/eigenfns_gb300.h"
+#include "status.h"
+
+#include <atomic>
+
+namespace {
+thread_local std::string g_last_error;
+std::atomic<unsigned long long> g_launches{0};
+}
+
+void ef_count_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
+
+int ef_fail(int code, const char* msg) {
+  g_last_error = msg ? msg : "";
+  return code;
+}
+
+int ef_check_launch() {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return ef_fail(EF_ERR_CUDA, cudaGetErrorString(e));
+  return EF_OK;
+}
+
+extern "C" {
+
+const char* ef_version(void) { return "eigenfns_gb300 0.1.0 (sm_103a)"; }
+
+const char* ef_status_string(int status) {
+  switch (status) {
+    case EF_OK: return "ok";
+    case EF_ERR_INVALID: return "invalid argument";
+    case EF_ERR_UNSUPPORTED: return "unsupported grid size";
+    case EF_ERR_CUDA: return "CUDA error";
+    case EF_ERR_WORKSPACE: return "workspace too small";
+    case EF_ERR_NONFINITE: return "non-finite or non-positive input";
+    case EF_ERR_TOO_LARGE: return "size beyond the fixed maximum";
+    default: return "unknown status";
+  }
+}
+
+const char* ef_last_error(void) { return g_last_error.c_str(); }
+
+unsigned long long ef_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+}  // extern "C"

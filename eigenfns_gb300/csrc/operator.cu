@@ -1,0 +1,448 @@
+// Maxwell operator handle and the fused FFT pipeline entry points.
+//
+// Reference: eigenfns/operator.py (make_basis :44-79, _theta_block :82-95,
+// _precondition_block :98-101, _precondition_fancy_block :104-127,
+// MaxwellOperator :130-184), the Chebyshev recurrence of
+// eigenfns/interior.py:336-354 and the KPM recurrences of
+// eigenfns/chebyshev.py:254-263 and scripts/exp/exp_kpm_dos.py:141-152.
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "fft_passes.cuh"
+#include "plan.cuh"
+#include "status.h"
+
+using namespace ef;
+
+namespace {
+
+const std::vector<Plan>& plans() {
+  static const std::vector<Plan> v = [] {
+    std::vector<Plan> p;
+    add_plans_small(p);
+    add_plans_mid(p);
+    add_plans_large(p);
+    return p;
+  }();
+  return v;
+}
+
+const Plan* find_plan(int G) {
+  for (const Plan& p : plans()) if (p.G == G) return &p;
+  return nullptr;
+}
+
+// ---- host-side fp64 frame tables (operator.py:46-59) -----------------------------
+void axis_wavevectors(int G, double L, const double k[3], std::vector<double>& K) {
+  // 2*pi*fftfreq(G, d=L/G) + 2*pi*k/L, evaluated in numpy's operation order
+  K.assign(3 * (size_t)G, 0.0);
+  const double d = L / G;
+  const double val = 1.0 / (G * d);
+  const int Np = (G - 1) / 2 + 1;
+  const double twopi = 2.0 * M_PI;
+  for (int ax = 0; ax < 3; ++ax) {
+    const double k0 = twopi * k[ax] / L;
+    for (int i = 0; i < G; ++i) {
+      long n = (i < Np) ? i : (long)i - G;
+      K[(size_t)ax * G + i] = twopi * ((double)n * val) + k0;
+    }
+  }
+}
+
+__global__ void basis_kernel(const float* kax, const uint32_t* swap, int G, float* kn, float* t,
+                             float* mask) {
+  const long long N = (long long)G * G * G;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+       i += (long long)gridDim.x * blockDim.x) {
+    int z = i % G, y = (i / G) % G, x = i / ((long long)G * G);
+    Frame f = frame_at(kax, swap, G, x, y, z);
+    if (kn) kn[i] = f.kn;
+    if (mask) mask[i] = f.kn > 0.f ? 1.f : 0.f;
+    if (t) {
+      t[0 * N + i] = f.t1x; t[1 * N + i] = f.t1y; t[2 * N + i] = f.t1z;
+      t[3 * N + i] = f.t2x; t[4 * N + i] = f.t2y; t[5 * N + i] = f.t2z;
+    }
+  }
+}
+
+__global__ void precond_simple_kernel(const float* kax, int G, const float2* X, float2* Y,
+                                      long long total, float scale) {
+  const long long N = (long long)G * G * G;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long vox = i % N;
+    int z = vox % G, y = (vox / G) % G, x = vox / ((long long)G * G);
+    float Kx = kax[x], Ky = kax[G + y], Kz = kax[2 * G + z];
+    float kn = sqrtf(Kx * Kx + Ky * Ky + Kz * Kz);
+    float d = kn * kn + scale;
+    float2 v = X[i];
+    Y[i] = make_float2(v.x / d, v.y / d);
+  }
+}
+
+// finalize per-vector sums of the pass-E partials (deterministic order)
+enum FinMode { FIN_KPM_FIRST = 0, FIN_KPM_STEP = 1, FIN_COUNT_FIRST = 2, FIN_COUNT_STEP = 3 };
+
+__global__ void finalize_kernel(const double* partials, int tiles, int mode, double* out, int ld,
+                                int k, double c0, double c1) {
+  __shared__ double r0[256], r1[256];
+  const int v = blockIdx.x;
+  double s0 = 0.0, s1 = 0.0;
+  for (int t = threadIdx.x; t < tiles; t += blockDim.x) {
+    s0 += partials[((long long)v * tiles + t) * 2];
+    s1 += partials[((long long)v * tiles + t) * 2 + 1];
+  }
+  r0[threadIdx.x] = s0;
+  r1[threadIdx.x] = s1;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) {
+      r0[threadIdx.x] += r0[threadIdx.x + o];
+      r1[threadIdx.x] += r1[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double d0 = r0[0], d1 = r1[0];
+    double* row = out + (long long)v * ld;
+    if (mode == FIN_KPM_FIRST) { row[0] = d0; row[1] = d1; }
+    else if (mode == FIN_KPM_STEP) { row[2 * k] = 2.0 * d0 - row[0]; row[2 * k + 1] = 2.0 * d1 - row[1]; }
+    else if (mode == FIN_COUNT_FIRST) { row[0] = c0 * d0 + c1 * d1; }
+    else { row[0] += c0 * d0; }
+  }
+}
+
+size_t subbatch_cap_bytes() {
+  const char* e = std::getenv("EF_SUBBATCH_BYTES");
+  if (e) {
+    long long v = std::atoll(e);
+    if (v > 0) return (size_t)v;
+  }
+  return (size_t)96 << 20;
+}
+
+struct Sizes {
+  long long N;
+  int tiles;
+  size_t per_vec;      // E bytes per vector
+  size_t per_vec_part; // partial bytes per vector
+};
+
+Sizes sizes_of(const ef_op* op, const Plan* p) {
+  Sizes s;
+  s.N = op->N;
+  s.tiles = (op->G * op->G) / p->NR;
+  s.per_vec = (size_t)3 * s.N * sizeof(float2);
+  s.per_vec_part = ((size_t)s.tiles * 2 * sizeof(double) + 255) / 256 * 256;
+  return s;
+}
+
+int mb_cap(const ef_op* op, const Sizes& s) {
+  size_t cap = subbatch_cap_bytes() / s.per_vec;
+  return cap < 1 ? 1 : (int)(cap > 4096 ? 4096 : cap);
+}
+
+struct Pipe {
+  int build;   // BuildMode
+  int wmode;   // WMode (0/1)
+  int epi;     // EpiMode
+  int fin;     // -1 none, else FinMode
+};
+
+// Run the 5-pass pipeline on m vectors in sub-batches.
+int run_pipe(const ef_op* op, const Pipe& pp, const float2* X, float2* out, float2* T0, float2* Y,
+             const float2* Z, int m, float s, float c0, float c1, double* fin_out, int fin_ld,
+             int fin_k, double fc0, double fc1, void* work, size_t work_bytes, cudaStream_t st) {
+  if (!op || m <= 0 || !X) return ef_fail(EF_ERR_INVALID, "null operator/input or m <= 0");
+  const Plan* p = find_plan(op->G);
+  if (!p) return ef_fail(EF_ERR_UNSUPPORTED, "no FFT plan for this grid");
+  Sizes sz = sizes_of(op, p);
+  if (!work) return ef_fail(EF_ERR_WORKSPACE, "work buffer is null");
+  int mb = mb_cap(op, sz);
+  if (mb > m) mb = m;
+  size_t need1 = sz.per_vec + sz.per_vec_part + 256;
+  if (work_bytes < need1) return ef_fail(EF_ERR_WORKSPACE, "work buffer smaller than one vector's workspace");
+  int fit = (int)((work_bytes - 256) / (sz.per_vec + sz.per_vec_part));
+  if (fit < mb) mb = fit;
+  float2* E = reinterpret_cast<float2*>(work);
+  size_t e_bytes = (size_t)mb * sz.per_vec;
+  double* partials = reinterpret_cast<double*>(reinterpret_cast<char*>(work) + (e_bytes + 255) / 256 * 256);
+  const int G = op->G, NR = p->NR, NZ = p->NZ, PS = p->PS;
+  const size_t smem_ae = (size_t)(2 * 3 * NR * PS + G) * sizeof(float2);
+  const size_t smem_y = (size_t)(NZ * PS + G) * sizeof(float2);
+  const size_t smem_c = (size_t)(2 * NZ * PS + G) * sizeof(float2);
+  const long long N2 = 2 * op->N;
+  for (int v0 = 0; v0 < m; v0 += mb) {
+    const int nb = (m - v0) < mb ? (m - v0) : mb;
+    PassArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.X = X + (long long)v0 * N2;
+    a.E = E;
+    a.out = out ? out + (long long)v0 * N2 : nullptr;
+    a.T0 = T0 ? T0 + (long long)v0 * N2 : nullptr;
+    a.Y = Y ? Y + (long long)v0 * N2 : nullptr;
+    a.Z = Z ? Z + (long long)v0 * N2 : nullptr;
+    a.partials = partials;
+    a.kax = op->kax;
+    a.swap = op->swap;
+    a.w = pp.wmode == W_EPS ? op->eps_n : op->inv_eps;
+    a.tw = op->tw;
+    a.inv_n = 1.0f / (float)op->N;
+    a.kn_floor = op->kn_floor;
+    a.s = s;
+    a.c0 = c0;
+    a.c1 = c1;
+    a.G = G;
+    p->a[pp.build](dim3(sz.tiles, nb), smem_ae, st, a);
+    p->y[0](dim3(G / NZ, G, 3 * nb), smem_y, st, a);
+    p->c[pp.wmode](dim3(G / NZ, G, 3 * nb), smem_c, st, a);
+    p->y[1](dim3(G / NZ, G, 3 * nb), smem_y, st, a);
+    p->e[pp.epi](dim3(sz.tiles, nb), smem_ae, st, a);
+    if (pp.fin >= 0) {
+      double* o = (pp.fin == FIN_COUNT_FIRST || pp.fin == FIN_COUNT_STEP) ? fin_out + v0 : fin_out + (long long)v0 * fin_ld;
+      ef_count_launches(1);
+      finalize_kernel<<<nb, 256, 0, st>>>(partials, sz.tiles, pp.fin, o, pp.fin >= FIN_COUNT_FIRST ? 1 : fin_ld, fin_k, fc0, fc1);
+    }
+  }
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return ef_fail(EF_ERR_CUDA, cudaGetErrorString(err));
+  return EF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ef_supported_grid(int grid) { return find_plan(grid) != nullptr; }
+
+int ef_op_create(int grid, double box_size, double kx, double ky, double kz, const float* eps_host,
+                 ef_op** out) {
+  if (!out) return ef_fail(EF_ERR_INVALID, "out is null");
+  *out = nullptr;
+  if (!eps_host || grid <= 0 || !(box_size > 0.0)) return ef_fail(EF_ERR_INVALID, "bad grid, box size or eps");
+  const Plan* p = find_plan(grid);
+  if (!p) return ef_fail(EF_ERR_UNSUPPORTED, "grid edge has no FFT plan");
+  if (!std::isfinite(kx) || !std::isfinite(ky) || !std::isfinite(kz))
+    return ef_fail(EF_ERR_INVALID, "non-finite k");
+  const int G = grid;
+  const long long N = (long long)G * G * G;
+  for (long long i = 0; i < N; ++i)
+    if (!std::isfinite(eps_host[i]) || !(eps_host[i] > 0.0f))
+      return ef_fail(EF_ERR_NONFINITE, "eps must be finite and positive");
+  ef_op* op = new ef_op();
+  std::memset(static_cast<ef::Op*>(op), 0, sizeof(ef::Op));
+  op->G = G; op->R1 = p->R1; op->R2 = p->R2; op->N = N; op->L = box_size;
+  op->k[0] = kx; op->k[1] = ky; op->k[2] = kz;
+  cudaGetDevice(&op->device);
+  std::vector<double> K;
+  axis_wavevectors(G, box_size, op->k, K);
+  std::vector<float> kaxf(3 * (size_t)G);
+  for (size_t i = 0; i < kaxf.size(); ++i) kaxf[i] = (float)K[i];
+  std::vector<uint32_t> swap((size_t)((N + 31) / 32), 0u);
+  double knmin = INFINITY;
+  for (int x = 0; x < G; ++x)
+    for (int y = 0; y < G; ++y)
+      for (int z = 0; z < G; ++z) {
+        double a0 = K[x], a1 = K[G + y], a2 = K[2 * G + z];
+        double kn = std::sqrt((a0 * a0 + a1 * a1) + a2 * a2);
+        bool sw = std::fabs(a2) > 0.9 * std::fmax(kn, 1e-300);
+        long long i = ((long long)x * G + y) * G + z;
+        if (sw) swap[i >> 5] |= (1u << (i & 31));
+        float knf = (float)kn;
+        if (knf > 0.0f && knf < knmin) knmin = knf;
+      }
+  op->kn_floor = (float)(0.5 * knmin);
+  std::vector<float> inv((size_t)N), epsn((size_t)N);
+  double acc = 0.0;
+  const float invN = (float)(1.0 / (double)N);
+  for (long long i = 0; i < N; ++i) {
+    float ie = 1.0f / eps_host[i];
+    acc += ie;
+    inv[i] = ie * invN;
+    epsn[i] = eps_host[i] * invN;
+  }
+  op->eps_mean_inv = acc / (double)N;
+  std::vector<float2> tw(G);
+  for (int j = 0; j < G; ++j) {
+    double ang = 2.0 * M_PI * (double)j / (double)G;
+    tw[j] = make_float2((float)std::cos(ang), (float)std::sin(ang));
+  }
+  cudaError_t e = cudaSuccess;
+  e = cudaMalloc(&op->kax, kaxf.size() * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&op->swap, swap.size() * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&op->inv_eps, (size_t)N * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&op->eps_n, (size_t)N * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&op->eps_raw, (size_t)N * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&op->tw, (size_t)G * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMemcpy(op->kax, kaxf.data(), kaxf.size() * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(op->swap, swap.data(), swap.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(op->inv_eps, inv.data(), (size_t)N * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(op->eps_n, epsn.data(), (size_t)N * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(op->eps_raw, eps_host, (size_t)N * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(op->tw, tw.data(), (size_t)G * sizeof(float2), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    ef_op_destroy(op);
+    return ef_fail(EF_ERR_CUDA, cudaGetErrorString(e));
+  }
+  *out = op;
+  return EF_OK;
+}
+
+int ef_op_destroy(ef_op* op) {
+  if (!op) return EF_OK;
+  cudaFree(op->kax);
+  cudaFree(op->swap);
+  cudaFree(op->inv_eps);
+  cudaFree(op->eps_n);
+  cudaFree(op->eps_raw);
+  cudaFree(op->tw);
+  delete op;
+  return EF_OK;
+}
+
+int ef_op_info(const ef_op* op, int* grid, double* kn_floor, double* eps_mean_inv) {
+  if (!op) return ef_fail(EF_ERR_INVALID, "null operator");
+  if (grid) *grid = op->G;
+  if (kn_floor) *kn_floor = op->kn_floor;
+  if (eps_mean_inv) *eps_mean_inv = op->eps_mean_inv;
+  return EF_OK;
+}
+
+int ef_op_basis(const ef_op* op, float* kn_dev, float* t_dev, void* stream) {
+  if (!op) return ef_fail(EF_ERR_INVALID, "null operator");
+  ef_count_launches(1);
+  basis_kernel<<<1024, 256, 0, (cudaStream_t)stream>>>(op->kax, op->swap, op->G, kn_dev, t_dev, nullptr);
+  return ef_check_launch();
+}
+
+int ef_op_mask(const ef_op* op, float* mask_dev, void* stream) {
+  if (!op || !mask_dev) return ef_fail(EF_ERR_INVALID, "null argument");
+  ef_count_launches(1);
+  basis_kernel<<<1024, 256, 0, (cudaStream_t)stream>>>(op->kax, op->swap, op->G, nullptr, nullptr, mask_dev);
+  return ef_check_launch();
+}
+
+size_t ef_op_workspace_bytes(const ef_op* op, int m) {
+  if (!op || m <= 0) return 0;
+  const Plan* p = find_plan(op->G);
+  if (!p) return 0;
+  Sizes sz = sizes_of(op, p);
+  int mb = mb_cap(op, sz);
+  if (mb > m) mb = m;
+  return (size_t)mb * (sz.per_vec + sz.per_vec_part) + 512;
+}
+
+int ef_theta(const ef_op* op, const float* X, float* Y, int m, void* work, size_t work_bytes,
+             void* stream) {
+  if (!Y) return ef_fail(EF_ERR_INVALID, "null output");
+  Pipe pp{BUILD_THETA, W_INV_EPS, EPI_THETA, -1};
+  return run_pipe(op, pp, (const float2*)X, (float2*)Y, nullptr, nullptr, nullptr, m, 0.f, 0.f,
+                  0.f, nullptr, 0, 0, 0.0, 0.0, work, work_bytes, (cudaStream_t)stream);
+}
+
+int ef_precondition(const ef_op* op, const float* X, float* Y, int m, void* work,
+                    size_t work_bytes, void* stream) {
+  if (!Y) return ef_fail(EF_ERR_INVALID, "null output");
+  Pipe pp{BUILD_PRECOND, W_EPS, EPI_PRECOND, -1};
+  return run_pipe(op, pp, (const float2*)X, (float2*)Y, nullptr, nullptr, nullptr, m, 0.f, 0.f,
+                  0.f, nullptr, 0, 0, 0.0, 0.0, work, work_bytes, (cudaStream_t)stream);
+}
+
+int ef_precondition_simple(const ef_op* op, const float* X, float* Y, int m, float scale,
+                           void* stream) {
+  if (!op || !X || !Y || m <= 0) return ef_fail(EF_ERR_INVALID, "null argument or m <= 0");
+  long long total = (long long)m * 2 * op->N;
+  ef_count_launches(1);
+  precond_simple_kernel<<<2048, 256, 0, (cudaStream_t)stream>>>(op->kax, op->G, (const float2*)X,
+                                                                 (float2*)Y, total, scale);
+  return ef_check_launch();
+}
+
+static int realspace(const ef_op* op, const float* X, float* out, const float* vscale, int m,
+                     int build, int wmode, cudaStream_t st) {
+  if (!op || !X || !out || m <= 0) return ef_fail(EF_ERR_INVALID, "null argument or m <= 0");
+  const Plan* p = find_plan(op->G);
+  if (!p) return ef_fail(EF_ERR_UNSUPPORTED, "no FFT plan for this grid");
+  const int G = op->G, NR = p->NR, NZ = p->NZ, PS = p->PS;
+  PassArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.X = (const float2*)X;
+  a.E = (float2*)out;
+  a.kax = op->kax;
+  a.swap = op->swap;
+  a.w = op->inv_eps;
+  a.tw = op->tw;
+  a.vscale = vscale;
+  a.inv_n = 1.0f / (float)op->N;
+  a.kn_floor = op->kn_floor;
+  a.G = G;
+  const int tiles = G * G / NR;
+  p->a[build](dim3(tiles, m), (size_t)(2 * 3 * NR * PS + G) * sizeof(float2), st, a);
+  p->y[0](dim3(G / NZ, G, 3 * m), (size_t)(NZ * PS + G) * sizeof(float2), st, a);
+  p->c[wmode](dim3(G / NZ, G, 3 * m), (size_t)(2 * NZ * PS + G) * sizeof(float2), st, a);
+  return ef_check_launch();
+}
+
+int ef_h_realspace(const ef_op* op, const float* X, float* H, int m, void* stream) {
+  return realspace(op, X, H, nullptr, m, BUILD_CART, W_INV_ONLY, (cudaStream_t)stream);
+}
+
+int ef_e_realspace(const ef_op* op, const float* X, const float* vec_scale_dev, float* Eout, int m,
+                   void* stream) {
+  if (!vec_scale_dev) return ef_fail(EF_ERR_INVALID, "null vec_scale");
+  return realspace(op, X, Eout, vec_scale_dev, m, BUILD_THETA, W_INV_ONLY_EPS, (cudaStream_t)stream);
+}
+
+int ef_cheb_first(const ef_op* op, const float* T0, float* T1, float* Y, int m, double s, float c0,
+                  float c1, void* work, size_t work_bytes, void* stream) {
+  if (!T1 || !Y) return ef_fail(EF_ERR_INVALID, "null output");
+  Pipe pp{BUILD_THETA, W_INV_EPS, EPI_CHEB_FIRST, -1};
+  return run_pipe(op, pp, (const float2*)T0, (float2*)T1, nullptr, (float2*)Y, nullptr, m, (float)s,
+                  c0, c1, nullptr, 0, 0, 0.0, 0.0, work, work_bytes, (cudaStream_t)stream);
+}
+
+int ef_cheb_step(const ef_op* op, const float* T1, float* T0, float* Y, int m, double s, float ck,
+                 void* work, size_t work_bytes, void* stream) {
+  if (!T0 || !Y) return ef_fail(EF_ERR_INVALID, "null output");
+  Pipe pp{BUILD_THETA, W_INV_EPS, EPI_CHEB, -1};
+  return run_pipe(op, pp, (const float2*)T1, nullptr, (float2*)T0, (float2*)Y, nullptr, m, (float)s,
+                  0.f, ck, nullptr, 0, 0, 0.0, 0.0, work, work_bytes, (cudaStream_t)stream);
+}
+
+int ef_kpm_first(const ef_op* op, const float* Z, float* T1, int m, double s, double* mom, int ld_mom,
+                 void* work, size_t work_bytes, void* stream) {
+  if (!T1 || !mom || ld_mom < 2) return ef_fail(EF_ERR_INVALID, "bad output arguments");
+  Pipe pp{BUILD_THETA, W_INV_EPS, EPI_KPM_FIRST, FIN_KPM_FIRST};
+  return run_pipe(op, pp, (const float2*)Z, (float2*)T1, nullptr, nullptr, nullptr, m, (float)s, 0.f,
+                  0.f, mom, ld_mom, 0, 0.0, 0.0, work, work_bytes, (cudaStream_t)stream);
+}
+
+int ef_kpm_step(const ef_op* op, const float* T1, float* T0, int m, double s, int k, double* mom,
+                int ld_mom, void* work, size_t work_bytes, void* stream) {
+  if (!T0 || !mom || k < 1 || ld_mom < 2 * k + 2) return ef_fail(EF_ERR_INVALID, "bad output arguments");
+  Pipe pp{BUILD_THETA, W_INV_EPS, EPI_KPM, FIN_KPM_STEP};
+  return run_pipe(op, pp, (const float2*)T1, nullptr, (float2*)T0, nullptr, nullptr, m, (float)s, 0.f,
+                  0.f, mom, ld_mom, k, 0.0, 0.0, work, work_bytes, (cudaStream_t)stream);
+}
+
+int ef_kpm_count_first(const ef_op* op, const float* Z, float* T1, int m, double s, double c0,
+                       double c1, double* est, void* work, size_t work_bytes, void* stream) {
+  if (!T1 || !est) return ef_fail(EF_ERR_INVALID, "bad output arguments");
+  Pipe pp{BUILD_THETA, W_INV_EPS, EPI_KPM_FIRST, FIN_COUNT_FIRST};
+  return run_pipe(op, pp, (const float2*)Z, (float2*)T1, nullptr, nullptr, nullptr, m, (float)s, 0.f,
+                  0.f, est, 1, 0, c0, c1, work, work_bytes, (cudaStream_t)stream);
+}
+
+int ef_kpm_count_step(const ef_op* op, const float* T1, float* T0, const float* Z, int m, double s,
+                      double ck, double* est, void* work, size_t work_bytes, void* stream) {
+  if (!T0 || !Z || !est) return ef_fail(EF_ERR_INVALID, "bad arguments");
+  Pipe pp{BUILD_THETA, W_INV_EPS, EPI_KPM_COUNT, FIN_COUNT_STEP};
+  return run_pipe(op, pp, (const float2*)T1, nullptr, (float2*)T0, nullptr, (const float2*)Z, m,
+                  (float)s, 0.f, 0.f, est, 1, 0, ck, 0.0, work, work_bytes, (cudaStream_t)stream);
+}
+
+}  // extern "C"

@@ -116,6 +116,7 @@ class SolveStats:
     theta_applications: int = 0
     rounds: list = field(default_factory=list)
     wall_seconds: float = 0.0
+    timeline: list = field(default_factory=list)   # (event, perf_counter)
 
 
 def rand_block(op, seed: int, stream: int, n: int):
@@ -156,6 +157,7 @@ def lobpcg_blocks(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
         X = ortho_block(deflate(X, locked, chunk_rows))
         HX = apply_chunked(op.theta, X, theta_chunk)
         stats.theta_applications += m
+        stats.timeline.append(("block_ready", time.perf_counter()))
         P = None
         n_lock = min(m - guard, nev - locked_vals.size)
         it = 0
@@ -173,6 +175,7 @@ def lobpcg_blocks(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
             if max_iters_total is not None and iters_total >= max_iters_total:
                 break
             iters_total += 1
+            stats.timeline.append(("iter_start", time.perf_counter()))
             W = (apply_chunked(op.precondition, R, theta_chunk) * mask).astype(op.dtype)
             del R
             W = deflate(W, locked, chunk_rows)
@@ -218,6 +221,7 @@ def lobpcg_blocks(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
             X = Xn
             HX = apply_chunked(op.theta, X, theta_chunk)
             stats.theta_applications += m
+            stats.timeline.append(("iter_end", time.perf_counter()))
         HX = apply_chunked(op.theta, X, theta_chunk)
         stats.theta_applications += m
         lam = rayleigh(X, HX, normalize_rq)

@@ -1,0 +1,236 @@
+"""GPU parity of the fused operator kernels against the reference's outputs and the oracle.
+
+Tolerances: complex64 arithmetic, so operator outputs are compared to the
+reference's complex128 results at a relative (max-norm) error below 5e-6 and
+to its complex64 results below 5e-6; analytic spectra at 5e-6 as in the
+reference's tests/test_operator.py:27-65.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def rel(a, b):
+    a = a.detach().cpu().numpy() if hasattr(a, "detach") else np.asarray(a)
+    b = np.asarray(b)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    from eigenfns_gb300 import _lib
+    _lib.load()
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    return torch.device("cuda", 0)
+
+
+def make_op(eps, L, k=(0.0, 0.0, 0.0)):
+    from eigenfns_gb300.operator import MaxwellOperator
+    return MaxwellOperator(eps, L, k_frac=k)
+
+
+@pytest.mark.parametrize("tag", ["op8", "op6k", "op12k"])
+def test_operator_matches_reference_outputs(golden, gpu, tag):
+    op = make_op(golden[f"{tag}_eps"], float(golden[f"{tag}_L"]), tuple(golden[f"{tag}_k"]))
+    X = golden[f"{tag}_X"].astype(np.complex64)
+    for name, fn in (("theta", lambda x: op.theta(x)), ("precond", lambda x: op.precondition(x)),
+                     ("precond_simple", lambda x: op.precondition_simple(x, 3.0)),
+                     ("h", lambda x: op.h_realspace(x)),
+                     ("e", lambda x: op.e_realspace(x, np.asarray([2.0, 3.0, 5.0])))):
+        out = fn(X)
+        assert rel(out, golden[f"{tag}_c128_{name}"]) < 5e-6, name
+        assert rel(out, golden[f"{tag}_c64_{name}"]) < 5e-6, name
+    assert op.kn_floor == pytest.approx(float(golden[f"{tag}_c64_kn_floor"]), rel=1e-7)
+    assert op.eps_mean_inv == pytest.approx(float(golden[f"{tag}_c64_eps_mean_inv"]), rel=1e-12)
+
+
+@pytest.mark.parametrize("tag", ["b0", "b1", "b2", "b3"])
+def test_basis_matches_reference(golden, gpu, tag):
+    G, L, k = int(golden[f"basis_{tag}_G"]), float(golden[f"basis_{tag}_L"]), golden[f"basis_{tag}_k"]
+    op = make_op(np.ones((G, G, G), np.float32), L, tuple(k))
+    assert np.abs(op.basis.kn.cpu().numpy() - golden[f"basis_{tag}_kn"]).max() < 2e-6 * golden[f"basis_{tag}_kn"].max()
+    assert np.abs(op.basis.t.cpu().numpy() - golden[f"basis_{tag}_t"]).max() < 2e-6
+    assert np.array_equal(op.mask.cpu().numpy() > 0, golden[f"basis_{tag}_kn"] > 0)
+
+
+@pytest.mark.parametrize("G,k,m", [(16, (0.0, 0.0, 0.0), 3), (24, (0.3, -0.1, 0.2), 2),
+                                   (32, (0.17, 0.41, -0.5), 5), (48, (0.0, 0.0, 0.0), 2),
+                                   (64, (0.25, 0.0, -0.125), 2), (96, (0.0, 0.0, 0.0), 1),
+                                   (128, (0.1, 0.2, 0.3), 1)])
+def test_operator_matches_oracle_every_plan(gpu, G, k, m):
+    from oracle.operator import MaxwellOperator as Ref
+    rng = np.random.default_rng(G)
+    eps = np.asarray(1.0 + 7.41 * (rng.random((G, G, G)) > 0.75), np.float32)
+    L = 1.7
+    X = (rng.standard_normal((m, 2, G, G, G)) + 1j * rng.standard_normal((m, 2, G, G, G))).astype(np.complex64)
+    ref = Ref(eps, L, k_frac=k, dtype=np.complex128)
+    op = make_op(eps, L, k)
+    assert rel(op.theta(X), ref.theta(X.astype(np.complex128))) < 5e-6
+    assert rel(op.precondition(X), ref.precondition(X.astype(np.complex128))) < 5e-6
+
+
+@pytest.mark.parametrize("G", [192, 256])
+def test_operator_large_plans_match_oracle(gpu, G):
+    from oracle.operator import MaxwellOperator as Ref
+    rng = np.random.default_rng(G)
+    eps = np.asarray(1.0 + 7.41 * (rng.random((G, G, G)) > 0.78), np.float32)
+    X = (rng.standard_normal((1, 2, G, G, G)) + 1j * rng.standard_normal((1, 2, G, G, G))).astype(np.complex64)
+    ref = Ref(eps, 10.0, dtype=np.complex64)
+    op = make_op(eps, 10.0)
+    assert rel(op.theta(X), ref.theta(X)) < 5e-6
+
+
+def _dense(op):
+    G = op.grid_size
+    n = 2 * G ** 3
+    I = torch.eye(n, dtype=torch.complex64, device=op.device).reshape(n, 2, G, G, G)
+    M = op.theta(I).reshape(n, n).T.cpu().numpy().astype(np.complex128)
+    return M
+
+
+def test_homogeneous_matches_analytic(gpu):
+    G, L, eps0 = 8, 1.0, 4.0
+    M = _dense(make_op(np.full((G, G, G), eps0, np.float32), L))
+    w = np.linalg.eigvalsh((M + M.conj().T) / 2)
+    k = 2 * np.pi * np.fft.fftfreq(G, d=L / G)
+    g2 = (np.array(np.meshgrid(k, k, k, indexing="ij")) ** 2).sum(0).ravel()
+    ana = np.sort(np.concatenate([g2[g2 > 0] / eps0] * 2))
+    assert (np.abs(w) < 1e-5).sum() == 2
+    assert (np.abs(np.sort(w)[2:] - ana) / ana).max() < 5e-6
+
+
+def test_hermitian_and_psd_on_disordered(gpu):
+    rng = np.random.default_rng(0)
+    G = 8
+    eps = np.asarray(1.0 + 7.57 * (rng.random((G, G, G)) > 0.7), np.float32)
+    M = _dense(make_op(eps, 1.0))
+    assert np.abs(M - M.conj().T).max() / np.abs(M).max() < 1e-5
+    w = np.linalg.eigvalsh((M + M.conj().T) / 2)
+    assert w.min() > -1e-4 * abs(w).max()
+
+
+def test_bloch_k_reduces_to_shifted_planewaves(gpu):
+    G, L, eps0 = 6, 1.0, 2.25
+    kf = (0.5, 0.0, 0.0)
+    M = _dense(make_op(np.full((G, G, G), eps0, np.float32), L, kf))
+    w = np.sort(np.linalg.eigvalsh((M + M.conj().T) / 2))
+    k1 = 2 * np.pi * np.fft.fftfreq(G, d=L / G)
+    k0 = 2 * np.pi * np.asarray(kf) / L
+    KX, KY, KZ = np.meshgrid(k1 + k0[0], k1 + k0[1], k1 + k0[2], indexing="ij")
+    ana = np.sort(np.concatenate([(KX ** 2 + KY ** 2 + KZ ** 2).ravel() / eps0] * 2))
+    assert (np.abs(w - ana) / np.maximum(ana, 1e-12)).max() < 5e-6
+
+
+def test_subbatching_and_errors(gpu, monkeypatch):
+    rng = np.random.default_rng(3)
+    G = 16
+    eps = np.asarray(1.0 + 3.0 * (rng.random((G, G, G)) > 0.5), np.float32)
+    X = torch.from_numpy((rng.standard_normal((7, 2, G, G, G)) + 1j * rng.standard_normal((7, 2, G, G, G))).astype(np.complex64)).cuda()
+    op = make_op(eps, 1.0)
+    full = op.theta(X)
+    for i in range(7):  # each vector alone gives the same result (per-vector independence)
+        assert torch.equal(op.theta(X[i:i + 1]), full[i:i + 1])
+    from eigenfns_gb300 import _lib
+    lib = _lib.load()
+    Y = torch.empty_like(X)
+    small = torch.empty(1024, dtype=torch.uint8, device=X.device)
+    with pytest.raises(ValueError):
+        _lib.call("ef_theta", op.handle, X.data_ptr(), Y.data_ptr(), 7, small.data_ptr(), small.numel(), None)
+    with pytest.raises(ValueError):
+        make_op(np.ones((7, 7, 7), np.float32), 1.0)
+    with pytest.raises(ValueError):
+        make_op(np.ones((8, 8, 4), np.float32), 1.0)
+    with pytest.raises(ValueError):
+        make_op(np.zeros((8, 8, 8), np.float32), 1.0)
+
+
+def test_random_blocks_match_oracle_generator(gpu):
+    from oracle.rng import complex_normal, rademacher
+    from eigenfns_gb300.chebyshev import random_block
+    from eigenfns_gb300._lib import EF_RAND_RADEMACHER, EF_RAND_RADEMACHER_C
+    G = 8
+    op = make_op(np.ones((G, G, G), np.float32), 1.0)
+    mask = op.mask.cpu().numpy()[None, None]
+    Z = random_block(op, 3, 11, 5).cpu().numpy()
+    ref = complex_normal(11, 5, (3, 2, G, G, G)) * mask
+    assert np.abs(Z - ref).max() < 1e-5
+    for kind, name in ((EF_RAND_RADEMACHER, "real"), (EF_RAND_RADEMACHER_C, "complex")):
+        Z = random_block(op, 2, 4, 9, kind).cpu().numpy()
+        assert np.array_equal(Z, rademacher(4, 9, (2, 2, G, G, G), name) * mask)
+
+
+def test_block_linear_algebra_matches_reference(golden, gpu):
+    from eigenfns_gb300 import blas, solver
+    dev = gpu
+    A, B, L, C = (torch.from_numpy(golden[k]).to(dev) for k in ("la_A", "la_B", "la_L", "la_C"))
+    assert rel(blas.gram(A, B), golden["la_gram"]) < 1e-6
+    assert rel(blas.combine(golden["la_C"], A, B), golden["la_combine"]) < 1e-6
+    assert rel(blas.deflate(B.clone(), L, 3), golden["la_deflate"]) < 1e-6
+    # SVQB output is defined up to the phases of the Gram eigenvectors: compare spans and
+    # orthonormality, not elements
+    O = solver.ortho_block(B).reshape(7, -1).cpu().numpy().astype(np.complex128)
+    R = golden["la_ortho"].reshape(7, -1).astype(np.complex128)
+    assert np.abs(O.conj() @ O.T - np.eye(7)).max() < 1e-5
+    s = np.linalg.svd(np.linalg.qr(O.T)[0].conj().T @ np.linalg.qr(R.T)[0], compute_uv=False)
+    assert s.min() > 1 - 1e-6
+    d = blas.rowdot(A, B).cpu().numpy()
+    ref = np.sum(golden["la_A"].reshape(5, -1).conj() * golden["la_B"][:5].reshape(5, -1), axis=1)
+    assert np.abs(d - ref).max() < 1e-6 * np.abs(ref).max() + 1e-3
+
+
+def test_gram_large_k_fp64_accuracy(gpu):
+    """Split-K with fp64 reduction: the Gram of unit vectors at K = 4.2M is exact to ~1e-7."""
+    g = torch.Generator(device="cuda").manual_seed(0)
+    K = 2 * 128 ** 3
+    X = torch.randn((8, K), dtype=torch.complex64, device="cuda", generator=g)
+    X = X / X.abs().pow(2).sum(1, keepdim=True).sqrt()
+    from eigenfns_gb300 import blas
+    Gm = blas.gram(X, X).cpu().numpy()
+    Xd = X.cpu().numpy().astype(np.complex128)
+    ref = Xd.conj() @ Xd.T
+    assert np.abs(Gm - ref).max() < 1e-7
+
+
+def test_rowstats_inplace_rotate_and_alias_rules(gpu):
+    from eigenfns_gb300 import blas
+    rng = np.random.default_rng(5)
+    K = 2 * 16 ** 3
+    A = (rng.standard_normal((5, K)) + 1j * rng.standard_normal((5, K))).astype(np.complex64)
+    B = (rng.standard_normal((5, K)) + 1j * rng.standard_normal((5, K))).astype(np.complex64)
+    At, Bt = torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()
+    st = blas.rowstats(At, Bt).cpu().numpy()
+    d = np.sum(A.astype(np.complex128).conj() * B, axis=1)
+    assert np.allclose(st[:, 0], d.real, rtol=1e-6) and np.allclose(st[:, 1], d.imag, rtol=1e-5, atol=1e-3)
+    assert np.allclose(st[:, 2], (np.abs(A.astype(np.complex128)) ** 2).sum(1), rtol=1e-6)
+    assert np.allclose(st[:, 3], (np.abs(B.astype(np.complex128)) ** 2).sum(1), rtol=1e-6)
+    # odd row length takes the scalar path
+    st2 = blas.rowstats(At[:, :K - 1].contiguous(), Bt[:, :K - 1].contiguous()).cpu().numpy()
+    d2 = np.sum(A[:, :K - 1].astype(np.complex128).conj() * B[:, :K - 1], axis=1)
+    assert np.allclose(st2[:, 0], d2.real, rtol=1e-6)
+    C = (rng.standard_normal((5, 5)) + 1j * rng.standard_normal((5, 5))).astype(np.complex64)
+    ref = (C.T.astype(np.complex128) @ A.astype(np.complex128))
+    X = At.clone()
+    blas.rotate(C, X, X)                     # in place, m_out <= 32
+    assert np.abs(X.cpu().numpy() - ref).max() < 1e-5 * np.abs(ref).max()
+    big = torch.zeros((40, K), dtype=torch.complex64, device="cuda")
+    with pytest.raises(ValueError):
+        blas.rotate(np.ones((40, 40), np.complex64), big, big)   # m_out > 32 may not alias
+    with pytest.raises(ValueError):
+        blas.rotate(np.ones((5, 5), np.complex64), big[0:5], big[2:7])  # partial overlap
+
+
+@pytest.mark.parametrize("ma,mb,K", [(32, 32, 2 * 64 ** 3), (96, 96, 2 * 32 ** 3), (7, 45, 1001),
+                                     (24, 200, 2 * 24 ** 3 + 1)])
+def test_gram_shapes_match_numpy(gpu, ma, mb, K):
+    from eigenfns_gb300 import blas
+    rng = np.random.default_rng(ma + mb)
+    A = (rng.standard_normal((ma, K)) + 1j * rng.standard_normal((ma, K))).astype(np.complex64)
+    B = (rng.standard_normal((mb, K)) + 1j * rng.standard_normal((mb, K))).astype(np.complex64)
+    got = blas.gram(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()).cpu().numpy()
+    ref = A.astype(np.complex128).conj() @ B.astype(np.complex128).T
+    assert np.abs(got - ref).max() < 2e-6 * np.abs(ref).max()
