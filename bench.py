@@ -238,6 +238,7 @@ def run_ours(args, w):
     launches0 = lib.ef_launch_count()
     starts, ends, stats_list, vals_list = [], [], [], []
     stream = torch.cuda.current_stream()
+    torch.cuda.nvtx.range_push("timed")
     with profiling.theta_timer() as tt:
         for _ in range(args.steps):
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -250,6 +251,7 @@ def run_ours(args, w):
             vals_list.append(vals)
             del vecs
         barrier()
+    torch.cuda.nvtx.range_pop()
     launches = int(lib.ef_launch_count() - launches0)
     clocks = sampler.stop()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]

@@ -56,6 +56,7 @@ SIGNATURES = {
     "ef_rowdot": (_i, [_vp, _vp, _i, _ll, _vp, _vp, _sz, _vp]),
     "ef_rowstats": (_i, [_vp, _vp, _i, _ll, _vp, _vp, _sz, _vp]),
     "ef_residual": (_i, [_vp, _vp, _vp, _vp, _i, _ll, _vp]),
+    "ef_residual_norms": (_i, [_vp, _vp, _vp, _vp, _i, _ll, _vp, _vp, _sz, _vp]),
     "ef_scale_rows": (_i, [_vp, _vp, _i, _ll, _vp]),
     "ef_axpby": (_i, [_vp, _vp, _ll, _d, _d, _vp]),
     "ef_rand_block": (_i, [_vp, _vp, _i, _u64, _u64, _i, _vp]),

@@ -136,6 +136,19 @@ def residual(HX: torch.Tensor, X: torch.Tensor, lam: torch.Tensor, out: torch.Te
     return out
 
 
+def residual_norms(HX: torch.Tensor, X: torch.Tensor, lam: torch.Tensor, out: torch.Tensor):
+    """out = HX - lam X (in place into `out`); returns |out_i|^2 (float64 device)."""
+    HX, X = _c64(HX), _c64(X)
+    m, K = _rows(X)
+    lam = lam.to(device=X.device, dtype=torch.float64).contiguous()
+    r2 = torch.empty((m,), dtype=torch.float64, device=X.device)
+    from ._lib import load
+    ws = workspace(load().ef_rowdot_workspace_bytes(m, K), X.device, "resnorm")
+    call("ef_residual_norms", HX.data_ptr(), X.data_ptr(), lam.data_ptr(), out.data_ptr(), m, K,
+         r2.data_ptr(), ws.data_ptr(), ws.numel(), _stream())
+    return r2
+
+
 def scale_rows(X: torch.Tensor, scale: torch.Tensor) -> torch.Tensor:
     """In place X_i *= scale[i]."""
     m, K = _rows(X)

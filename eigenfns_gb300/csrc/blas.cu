@@ -148,11 +148,12 @@ __global__ void __launch_bounds__(PG_THREADS) gram_pipe_kernel(const float2* __r
     }
     cp_async_commit();
   };
-  float accr[2][4], acci[2][4];
+  // two fp32 levels: a stage's 32 products, then the chunk's sum of stage sums
+  float accr[2][4], acci[2][4], totr[2][4], toti[2][4];
 #pragma unroll
   for (int r = 0; r < 2; ++r)
 #pragma unroll
-    for (int c = 0; c < 4; ++c) accr[r][c] = acci[r][c] = 0.f;
+    for (int c = 0; c < 4; ++c) accr[r][c] = acci[r][c] = totr[r][c] = toti[r][c] = 0.f;
   if (nst > 0) issue(0, 0);
   for (int st = 0; st < nst; ++st) {
     const int buf = st & 1;
@@ -177,6 +178,14 @@ __global__ void __launch_bounds__(PG_THREADS) gram_pipe_kernel(const float2* __r
         acci[1][c] = fmaf(a1.x, b[c].y, fmaf(-a1.y, b[c].x, acci[1][c]));
       }
     }
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        totr[r][c] += accr[r][c];
+        toti[r][c] += acci[r][c];
+        accr[r][c] = acci[r][c] = 0.f;
+      }
     __syncthreads();
   }
   double2* out = partial + (long long)blockIdx.z * ma * mb;
@@ -185,7 +194,7 @@ __global__ void __launch_bounds__(PG_THREADS) gram_pipe_kernel(const float2* __r
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
       int i = i0 + ti + 16 * r, j = j0 + tj + 8 * c;
-      if (i < ma && j < mb) out[(long long)i * mb + j] = make_double2((double)accr[r][c], (double)acci[r][c]);
+      if (i < ma && j < mb) out[(long long)i * mb + j] = make_double2((double)totr[r][c], (double)toti[r][c]);
     }
 }
 
@@ -216,8 +225,7 @@ constexpr int RT = 32;      // outputs per thread
 constexpr int RTHREADS = 256;
 
 __global__ void __launch_bounds__(RTHREADS) rotate_kernel(const float2* __restrict__ C,
-                                                          const float2* __restrict__ S,
-                                                          float2* __restrict__ out, int m_in,
+                                                          const float2* S, float2* out, int m_in,
                                                           int m_out, long long K, int mode) {
   extern __shared__ float2 Cs[];  // (m_in, RT) slice of C for this output tile
   const int i0 = blockIdx.y * RT;
@@ -271,26 +279,35 @@ __global__ void __launch_bounds__(DTHREADS) rowstats_kernel(const float4* __rest
   const float4* a = A + (long long)row * K2;
   const float4* b = B + (long long)row * K2;
   double s[4] = {0.0, 0.0, 0.0, 0.0};
-  float f[4] = {0.f, 0.f, 0.f, 0.f};
-  int cnt = 0;
-  for (long long k = kb + threadIdx.x; k < ke; k += blockDim.x) {
-    float4 x = a[k], y = b[k];
-    // two complex values per float4: (x.x + i x.y), (x.z + i x.w)
-    f[0] = fmaf(x.x, y.x, fmaf(x.y, y.y, fmaf(x.z, y.z, fmaf(x.w, y.w, f[0]))));
-    f[1] = fmaf(x.x, y.y, fmaf(-x.y, y.x, fmaf(x.z, y.w, fmaf(-x.w, y.z, f[1]))));
-    f[2] = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, f[2]))));
-    f[3] = fmaf(y.x, y.x, fmaf(y.y, y.y, fmaf(y.z, y.z, fmaf(y.w, y.w, f[3]))));
-    if (++cnt == 32) {
+  constexpr int U = 4;
+  for (long long k0 = kb; k0 < ke; k0 += (long long)U * 8 * blockDim.x) {
+    // 8 rounds of U independent loads, summed in fp32, then flushed to fp64
+    float f[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 2
+    for (int r = 0; r < 8; ++r) {
+      float4 x[U], y[U];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) { s[q] += f[q]; f[q] = 0.f; }
-      cnt = 0;
+      for (int u = 0; u < U; ++u) {
+        long long k = k0 + ((long long)r * U + u) * blockDim.x + threadIdx.x;
+        bool ok = k < ke;
+        x[u] = ok ? a[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+        y[u] = ok ? b[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        float4 p = x[u], q = y[u];
+        f[0] = fmaf(p.x, q.x, fmaf(p.y, q.y, fmaf(p.z, q.z, fmaf(p.w, q.w, f[0]))));
+        f[1] = fmaf(p.x, q.y, fmaf(-p.y, q.x, fmaf(p.z, q.w, fmaf(-p.w, q.z, f[1]))));
+        f[2] = fmaf(p.x, p.x, fmaf(p.y, p.y, fmaf(p.z, p.z, fmaf(p.w, p.w, f[2]))));
+        f[3] = fmaf(q.x, q.x, fmaf(q.y, q.y, fmaf(q.z, q.z, fmaf(q.w, q.w, f[3]))));
+      }
     }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) s[q] += (double)f[q];
   }
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    s[q] += f[q];
+  for (int q = 0; q < 4; ++q)
     for (int o = 16; o > 0; o >>= 1) s[q] += __shfl_down_sync(0xffffffffu, s[q], o);
-  }
   if ((threadIdx.x & 31) == 0) {
 #pragma unroll
     for (int q = 0; q < 4; ++q) red[q][threadIdx.x >> 5] = s[q];
@@ -303,6 +320,64 @@ __global__ void __launch_bounds__(DTHREADS) rowstats_kernel(const float4* __rest
       for (int q = 0; q < 4; ++q) t[q] += red[q][w];
     partial[(long long)row * gridDim.x + blockIdx.x] = make_double4(t[0], t[1], t[2], t[3]);
   }
+}
+
+// R = HX - lam[row] X and |R|^2 per row (fp32 runs flushed to fp64)
+__global__ void __launch_bounds__(DTHREADS) residual_norm_kernel(const float4* __restrict__ HX,
+                                                                 const float4* __restrict__ X,
+                                                                 const double* __restrict__ lam,
+                                                                 float4* R, long long K2,
+                                                                 long long kchunk, double* partial) {
+  __shared__ double red[DTHREADS / 32];
+  const int row = blockIdx.y;
+  const long long kb = (long long)blockIdx.x * kchunk;
+  long long ke = kb + kchunk;
+  if (ke > K2) ke = K2;
+  const float l = (float)lam[row];
+  const float4* h = HX + (long long)row * K2;
+  const float4* x = X + (long long)row * K2;
+  float4* r = R + (long long)row * K2;
+  double s = 0.0;
+  constexpr int U = 4;
+  for (long long k0 = kb; k0 < ke; k0 += (long long)U * 8 * blockDim.x) {
+    float f = 0.f;
+#pragma unroll 2
+    for (int q = 0; q < 8; ++q) {
+      float4 hv[U], xv[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        long long k = k0 + ((long long)q * U + u) * blockDim.x + threadIdx.x;
+        bool ok = k < ke;
+        hv[u] = ok ? h[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+        xv[u] = ok ? x[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        long long k = k0 + ((long long)q * U + u) * blockDim.x + threadIdx.x;
+        float4 v = make_float4(hv[u].x - l * xv[u].x, hv[u].y - l * xv[u].y, hv[u].z - l * xv[u].z,
+                               hv[u].w - l * xv[u].w);
+        if (k < ke) r[k] = v;
+        f = fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, fmaf(v.w, v.w, f))));
+      }
+    }
+    s += (double)f;
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < DTHREADS / 32; ++w) t += red[w];
+    partial[(long long)row * gridDim.x + blockIdx.x] = t;
+  }
+}
+
+__global__ void sum_rows_kernel(const double* partial, int nchunk, int m, double* out) {
+  int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= m) return;
+  double t = 0.0;
+  for (int c = 0; c < nchunk; ++c) t += partial[(long long)row * nchunk + c];
+  out[row] = t;
 }
 
 __global__ void rowstats_reduce_kernel(const double4* partial, int nchunk, int m, double4* out) {
@@ -560,6 +635,25 @@ int ef_residual(const float* HX, const float* X, const double* lam, float* R, in
   ef_count_launches(1);
   residual_kernel<<<grid_for(total), 256, 0, (cudaStream_t)stream>>>((const float2*)HX, (const float2*)X,
                                                                       lam, (float2*)R, K, total);
+  return ef_check_launch();
+}
+
+int ef_residual_norms(const float* HX, const float* X, const double* lam, float* R, int m,
+                      long long K, double* r2, void* work, size_t work_bytes, void* stream) {
+  if (!HX || !X || !lam || !R || !r2 || m <= 0 || K <= 0)
+    return ef_fail(EF_ERR_INVALID, "bad residual_norms arguments");
+  if ((K % 2) != 0 || ((((uintptr_t)HX) | ((uintptr_t)X) | ((uintptr_t)R)) % 16) != 0)
+    return ef_fail(EF_ERR_INVALID, "residual_norms needs even K and 16-byte aligned rows");
+  int nc = rowdot_chunks(K);
+  if (!work || work_bytes < (size_t)m * nc * sizeof(double) + 256)
+    return ef_fail(EF_ERR_WORKSPACE, "residual_norms work buffer too small");
+  cudaStream_t st = (cudaStream_t)stream;
+  long long K2 = K / 2;
+  long long kchunk = (K2 + nc - 1) / nc;
+  ef_count_launches(2);
+  residual_norm_kernel<<<dim3(nc, m), DTHREADS, 0, st>>>((const float4*)HX, (const float4*)X, lam,
+                                                        (float4*)R, K2, kchunk, (double*)work);
+  sum_rows_kernel<<<(m + 127) / 128, 128, 0, st>>>((const double*)work, nc, m, r2);
   return ef_check_launch();
 }
 

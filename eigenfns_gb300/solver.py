@@ -108,11 +108,18 @@ def _normalize_rows(X: torch.Tensor, floor: float) -> None:
     blas.scale_rows(X, 1.0 / torch.clamp(torch.sqrt(torch.clamp(st[:, 2], min=0.0)), min=floor))
 
 
-def _residual_norms(st: np.ndarray, lam: np.ndarray) -> np.ndarray:
-    """|HX - lam X| / |HX| from the one-pass sums (fp64; no fp32 rounding of R)."""
-    d, xx, hh = st[:, 0], st[:, 2], st[:, 3]
-    r2 = np.maximum(hh - 2.0 * lam * d + lam * lam * xx, 0.0)
-    return np.sqrt(r2) / np.maximum(np.sqrt(np.maximum(hh, 0.0)), 1e-30)
+def _ritz_residuals(X, HX, R, normalize: bool):
+    """(lam, relres, |x|) for the rows of X, with R = HX - lam X written into `R`.
+
+    One pass for <x, Θx>, |x|^2, |Θx|^2 and one fused pass that forms R and |R|^2;
+    the small per-row vectors reach the host in a single copy."""
+    st = blas.rowstats(X, HX)
+    lam_d = st[:, 0] / torch.clamp(st[:, 2], min=1e-30) if normalize else st[:, 0].contiguous()
+    r2 = blas.residual_norms(HX, X, lam_d, R)
+    h = torch.cat([lam_d[:, None], st[:, 2:4], r2[:, None]], dim=1).cpu().numpy()
+    lam, xx, hh, rr = h[:, 0], h[:, 1], h[:, 2], h[:, 3]
+    rn = np.sqrt(np.maximum(rr, 0.0)) / np.maximum(np.sqrt(np.maximum(hh, 0.0)), 1e-30)
+    return lam, rn, np.sqrt(np.maximum(xx, 0.0))
 
 
 def lobpcg_blocks(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
@@ -172,10 +179,8 @@ def lobpcg_blocks(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
         n_lock = min(m - guard, nev - locked_vals.size)
         it = 0
         for it in range(maxit):
-            st = blas.rowstats(X, HX).cpu().numpy()
-            lam = st[:, 0].copy()
-            rn = _residual_norms(st, lam)
-            xnorm = np.sqrt(np.maximum(st[:, 2], 0))
+            # R = HX - lam X lands in the W slot, where the preconditioner needs it
+            lam, rn, xnorm = _ritz_residuals(X, HX, W, False)
             dead_rows = xnorm < 0.5
             lam_h = np.where(dead_rows, np.inf, lam)
             rn = np.where(dead_rows, np.inf, rn)
@@ -188,7 +193,6 @@ def lobpcg_blocks(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
                       f"{lo[-1]:.4f}  res q50/q90 {np.quantile(rn, 0.5):.1e}/{np.quantile(rn, 0.9):.1e}",
                       flush=True)
             stats.iterations += 1
-            blas.residual(HX, X, torch.from_numpy(lam).to(dev), out=W)
             op.precondition(W, out=W)
             deflate(W, locked, deflate_chunk)
             for _ in range(2):
@@ -236,10 +240,7 @@ def lobpcg_blocks(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
             _normalize_rows(S[0:2 * m], 1e-20)
             _theta(op, X, stats, out=HX)
         _theta(op, X, stats, out=HX)
-        st = blas.rowstats(X, HX).cpu().numpy()
-        lam = st[:, 0] / np.maximum(st[:, 2], 1e-30) if normalize_rq else st[:, 0].copy()
-        rn = _residual_norms(st, lam)
-        xnorm = np.sqrt(np.maximum(st[:, 2], 0))
+        lam, rn, xnorm = _ritz_residuals(X, HX, W, normalize_rq)
         lam = np.where(xnorm < 0.5, np.inf, lam)
         rn = np.where(xnorm < 0.5, np.inf, rn)
         order = np.argsort(lam)

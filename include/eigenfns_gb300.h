@@ -145,6 +145,10 @@ int ef_rowdot(const float* A, const float* B, int m, long long K, double* out,
 /* R = HX - lam[i] X_i with lam a device float64 (m) array (solver.py:229) */
 int ef_residual(const float* HX, const float* X, const double* lam, float* R, int m,
                 long long K, void* stream);
+/* R = HX - lam[i] X_i and r2[i] = |R_i|^2 (float64, device) in one pass; K even and
+ * 16-byte aligned rows; work >= ef_rowdot_workspace_bytes(m, K) (solver.py:229-231) */
+int ef_residual_norms(const float* HX, const float* X, const double* lam, float* R, int m,
+                      long long K, double* r2, void* work, size_t work_bytes, void* stream);
 /* X_i *= scale[i] (device float64 (m)) */
 int ef_scale_rows(float* X, const double* scale, int m, long long K, void* stream);
 /* Y = a X + b Y with real scalars (recurrence helpers, lanczos) */

@@ -122,10 +122,12 @@ def test_kpm_moments_match_oracle_complex_probes(gpu):
     from eigenfns_gb300.structure import make_structure
     from oracle.kpm import kpm_moments as ref_moments
     from oracle.operator import MaxwellOperator as Ref
+    from oracle.chebyshev import lanczos_lambda_max as ref_lanczos
     eps, L, _ = make_structure(64, 32, seed=5)
-    lam_max = 900.0
+    ref_op = Ref(eps, L, dtype=np.complex128)
+    lam_max = 1.05 * ref_lanczos(ref_op, iters=24, n_seeds=1)
     mom = kpm_moments(MaxwellOperator(eps, L), lam_max, 60, 3, seed=2, probe_kind="complex")
-    ref = ref_moments(Ref(eps, L, dtype=np.complex128), lam_max, 60, 3, seed=2, probe_kind="complex")
+    ref = ref_moments(ref_op, lam_max, 60, 3, seed=2, probe_kind="complex")
     assert np.abs(mom / mom[:, :1] - ref / ref[:, :1]).max() < 1e-4
 
 
