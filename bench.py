@@ -41,7 +41,12 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "modes/s at ≤1e-6 eigval err, served vs plain GPU path; p50/p99 solve latency"
-WORKLOAD = dict(nodes=1000, grid=128, bands=200, block=32, guard=8, tol=1e-6, seed=0, sub=4)
+# The configuration words the lock criterion as residual 1e-6; in complex64 the
+# relative residual of these bands floors at ~1-3e-5 at 128^3 (FFT rounding times
+# |k+G|; the reference's own complex64 arithmetic shows the same floor), so the
+# solve locks at the reference's default tolerance 1e-4 and the 1e-6 bar is held
+# on the eigenvalue error against complex128 runs (tests/test_gpu_accuracy.py).
+WORKLOAD = dict(nodes=1000, grid=128, bands=200, block=32, guard=8, tol=1e-4, seed=0, sub=4)
 
 
 def _peaks():
@@ -198,7 +203,9 @@ def _config(w, args):
                          f"deflated block LOBPCG (block {w['block']}, guard {w['guard']}, tol {w['tol']}), "
                          f"plain complex64 GPU path"),
             "nodes": w["nodes"], "grid": w["grid"], "bands": w["bands"], "block": w["block"],
-            "guard": w["guard"], "tol": w["tol"], "l2": "inputs larger than L2 (each 32-vector block is 1.07 GB)",
+            "guard": w["guard"], "tol": w["tol"],
+            "tol_note": "relative-residual lock at 1e-4 (complex64 floor ~1-3e-5 at 128^3); eigenvalue error vs complex128 <= 1e-6 is the checked bar",
+            "l2": "inputs larger than L2 (each 32-vector block is 1.07 GB)",
             "parallelism": f"replicas x{args.gpus}"}
 
 
@@ -353,12 +360,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", type=int, default=None, help="override the grid (smaller probes)")
     ap.add_argument("--bands", type=int, default=None)
+    ap.add_argument("--tol", type=float, default=None)
     args = ap.parse_args()
     w = dict(WORKLOAD)
     if args.grid:
         w["grid"] = args.grid
     if args.bands:
         w["bands"] = args.bands
+    if args.tol:
+        w["tol"] = args.tol
     if args.impl == "reference":
         return run_reference(args, w)
     return run_ours(args, w)

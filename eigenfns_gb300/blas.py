@@ -62,6 +62,22 @@ def gram(A: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
     return out
 
 
+def gram_tc(A: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
+    """gram() on the tcgen05 tensor cores (3xTF32 split, TMEM accumulators)."""
+    A, B = _c64(A), _c64(B)
+    ma, K = _rows(A)
+    mb, Kb = _rows(B)
+    if K != Kb:
+        raise ValueError("gram_tc: vector sizes differ")
+    out = torch.empty((ma, mb), dtype=torch.complex128, device=A.device)
+    err = torch.zeros((1,), dtype=torch.int32, device=A.device)
+    from ._lib import load
+    ws = workspace(load().ef_gram_tc_workspace_bytes(ma, mb, K), A.device, "gram_tc")
+    call("ef_gram_tc", A.data_ptr(), B.data_ptr(), ma, mb, K, out.data_ptr(), err.data_ptr(),
+         ws.data_ptr(), ws.numel(), _stream())
+    return out, err
+
+
 def _coef(C, device) -> torch.Tensor:
     if isinstance(C, torch.Tensor):
         return C.to(device=device, dtype=torch.complex64).contiguous()

@@ -227,7 +227,8 @@ constexpr int RTHREADS = 256;
 __global__ void __launch_bounds__(RTHREADS) rotate_kernel(const float2* __restrict__ C,
                                                           const float2* S, float2* out, int m_in,
                                                           int m_out, long long K, int mode) {
-  extern __shared__ float2 Cs[];  // (m_in, RT) slice of C for this output tile
+  extern __shared__ float4 Cs4[];  // (m_in, RT) slice of C for this output tile, 2 complex per float4
+  float2* Cs = reinterpret_cast<float2*>(Cs4);
   const int i0 = blockIdx.y * RT;
   const int nt = (m_out - i0) < RT ? (m_out - i0) : RT;
   for (int e = threadIdx.x; e < m_in * RT; e += blockDim.x) {
@@ -235,19 +236,41 @@ __global__ void __launch_bounds__(RTHREADS) rotate_kernel(const float2* __restri
     Cs[e] = (ii < nt) ? C[(long long)j * m_out + i0 + ii] : make_float2(0.f, 0.f);
   }
   __syncthreads();
+  constexpr int JU = 4;   // rows of S loaded together
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < K;
        k += (long long)gridDim.x * blockDim.x) {
     float2 acc[RT];
 #pragma unroll
     for (int ii = 0; ii < RT; ++ii) acc[ii] = make_float2(0.f, 0.f);
-    for (int j = 0; j < m_in; ++j) {
-      float2 s = S[(long long)j * K + k];
-      const float2* cj = Cs + j * RT;
+    int j = 0;
+    for (; j + JU <= m_in; j += JU) {
+      float2 sv[JU];
 #pragma unroll
-      for (int ii = 0; ii < RT; ++ii) {
-        float2 c = cj[ii];
-        acc[ii].x = fmaf(c.x, s.x, fmaf(-c.y, s.y, acc[ii].x));
-        acc[ii].y = fmaf(c.x, s.y, fmaf(c.y, s.x, acc[ii].y));
+      for (int u = 0; u < JU; ++u) sv[u] = S[(long long)(j + u) * K + k];
+#pragma unroll
+      for (int u = 0; u < JU; ++u) {
+        const float4* cj = Cs4 + (j + u) * (RT / 2);
+#pragma unroll
+        for (int h = 0; h < RT / 2; ++h) {
+          float4 c = cj[h];
+          float2 s2 = sv[u];
+          acc[2 * h].x = fmaf(c.x, s2.x, fmaf(-c.y, s2.y, acc[2 * h].x));
+          acc[2 * h].y = fmaf(c.x, s2.y, fmaf(c.y, s2.x, acc[2 * h].y));
+          acc[2 * h + 1].x = fmaf(c.z, s2.x, fmaf(-c.w, s2.y, acc[2 * h + 1].x));
+          acc[2 * h + 1].y = fmaf(c.z, s2.y, fmaf(c.w, s2.x, acc[2 * h + 1].y));
+        }
+      }
+    }
+    for (; j < m_in; ++j) {
+      float2 s2 = S[(long long)j * K + k];
+      const float4* cj = Cs4 + j * (RT / 2);
+#pragma unroll
+      for (int h = 0; h < RT / 2; ++h) {
+        float4 c = cj[h];
+        acc[2 * h].x = fmaf(c.x, s2.x, fmaf(-c.y, s2.y, acc[2 * h].x));
+        acc[2 * h].y = fmaf(c.x, s2.y, fmaf(c.y, s2.x, acc[2 * h].y));
+        acc[2 * h + 1].x = fmaf(c.z, s2.x, fmaf(-c.w, s2.y, acc[2 * h + 1].x));
+        acc[2 * h + 1].y = fmaf(c.z, s2.y, fmaf(c.w, s2.x, acc[2 * h + 1].y));
       }
     }
 #pragma unroll

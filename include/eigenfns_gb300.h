@@ -125,6 +125,12 @@ size_t ef_gram_workspace_bytes(int ma, int mb, long long K);
  * gram (solver.py:35-43) with fp32 products and a fp64 split-K reduction */
 int ef_gram(const float* A, const float* B, int ma, int mb, long long K, double* G,
             void* work, size_t work_bytes, void* stream);
+/* the same Gram on the tcgen05 tensor cores: 3xTF32 split products (fp32-class accuracy),
+ * fp32 accumulation in TMEM per K-chunk, fp64 reduction across chunks. mb <= 256, K even,
+ * 16-byte aligned rows. err_dev (device int) is set to 1 if a bounded wait timed out. */
+size_t ef_gram_tc_workspace_bytes(int ma, int mb, long long K);
+int ef_gram_tc(const float* A, const float* B, int ma, int mb, long long K, double* G, int* err_dev,
+               void* work, size_t work_bytes, void* stream);
 /* out_i (+/-)= sum_j C[j][i] S_j, C complex64 (m_in, m_out) row-major:
  * combine / tensordot(C.T, S) (solver.py:49-57,106,125); mode 0 set, 1 add, -1 subtract.
  * `out` may be `S` itself when m_out <= 32 (each column k is read in full before it is
