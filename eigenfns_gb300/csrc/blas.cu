@@ -12,6 +12,7 @@
 // fixed order, so results are deterministic and the long sums keep fp64 accuracy.
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 
 #include "common.cuh"
 #include "dft.cuh"
@@ -544,6 +545,40 @@ int grid_for(long long total) {
 
 }  // namespace
 
+// ---- Gram with a fixed scratch area owned by the library --------------------------
+// ef_gram_noalloc serves callers that have no way to hand the library device
+// scratch memory: a host program in another language whose only device memory is
+// the vectors it already owns, or a service running under a fixed device-memory
+// budget that forbids allocations after start-up. Its split-K partial sums live in
+// this file-scope array instead of a caller-provided work buffer. Every GPU that
+// loads the library holds the array until the process exits.
+constexpr size_t kNoallocScratchBytes = (size_t)8 << 20;   // 8 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kMaxDevices] = {nullptr};   // device address of the array, per device
+
+// The array's name in host code is only a stand-in: ask the runtime for its device
+// address, once per device, with that device current.
+int noalloc_scratch(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return ef_fail(EF_ERR_CUDA, cudaGetErrorString(e));
+  if (dev < 0 || dev >= kMaxDevices) return ef_fail(EF_ERR_INVALID, "device index out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) return ef_fail(EF_ERR_CUDA, "cudaGetSymbolAddress of the gram scratch failed");
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return EF_OK;
+}
+}  // namespace
+
 extern "C" {
 
 size_t ef_gram_workspace_bytes(int ma, int mb, long long K) {
@@ -573,6 +608,36 @@ int ef_gram(const float* A, const float* B, int ma, int mb, long long K, double*
   int n = ma * mb;
   ef_count_launches(1);
   gram_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>((const double2*)work, ns, n, (double2*)G);
+  return ef_check_launch();
+}
+
+int ef_gram_noalloc(const float* A, const float* B, int ma, int mb, long long K, double* G,
+                    void* stream) {
+  if (!A || !B || !G || ma <= 0 || mb <= 0 || K <= 0) return ef_fail(EF_ERR_INVALID, "bad gram arguments");
+  const size_t per_split = (size_t)ma * mb * sizeof(double2);
+  if (per_split > kNoallocScratchBytes)
+    return ef_fail(EF_ERR_TOO_LARGE, "gram_noalloc: ma*mb*16 bytes exceeds the fixed 8 MiB scratch");
+  void* scratch = nullptr;
+  int rc = noalloc_scratch(&scratch);
+  if (rc != EF_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  int ns = gram_splits(ma, mb, K);
+  const int cap = (int)(kNoallocScratchBytes / per_split);
+  if (ns > cap) ns = cap;
+  long long kchunk = (K + ns - 1) / ns;
+  kchunk = (kchunk + GBK - 1) / GBK * GBK;
+  ns = (int)((K + kchunk - 1) / kchunk);
+  dim3 grid((ma + GT - 1) / GT, (mb + GT - 1) / GT, ns);
+  const bool pipe = (K % 2 == 0) && ((((uintptr_t)A) | ((uintptr_t)B)) % 16 == 0);
+  ef_count_launches(2);
+  if (pipe)
+    gram_pipe_kernel<<<grid, PG_THREADS, 0, st>>>((const float2*)A, (const float2*)B, ma, mb, K,
+                                                  kchunk, (double2*)scratch);
+  else
+    gram_kernel<<<grid, GTHREADS, 0, st>>>((const float2*)A, (const float2*)B, ma, mb, K, kchunk,
+                                          (double2*)scratch);
+  int n = ma * mb;
+  gram_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>((const double2*)scratch, ns, n, (double2*)G);
   return ef_check_launch();
 }
 

@@ -125,6 +125,15 @@ size_t ef_gram_workspace_bytes(int ma, int mb, long long K);
  * gram (solver.py:35-43) with fp32 products and a fp64 split-K reduction */
 int ef_gram(const float* A, const float* B, int ma, int mb, long long K, double* G,
             void* work, size_t work_bytes, void* stream);
+/* ef_gram without a work buffer, for callers that cannot provide device scratch
+ * (no counterpart in the reference). The split-K partials use an 8 MiB array owned by
+ * the library, held on every GPU that loads it; ma*mb*16 must not exceed 8 MiB
+ * (EF_ERR_TOO_LARGE otherwise). The first call on a device looks up the array's device
+ * address; make that first call before any stream capture. All calls share the array:
+ * calls that can overlap on the GPU (other streams, other threads) race and must be
+ * serialised by the caller. Allocates nothing. */
+int ef_gram_noalloc(const float* A, const float* B, int ma, int mb, long long K, double* G,
+                    void* stream);
 /* the same Gram on the tcgen05 tensor cores: 3xTF32 split products (fp32-class accuracy),
  * fp32 accumulation in TMEM per K-chunk, fp64 reduction across chunks. mb <= 256, K even,
  * 16-byte aligned rows. err_dev (device int) is set to 1 if a bounded wait timed out. */
