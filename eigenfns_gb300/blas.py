@@ -23,13 +23,24 @@ def _stream():
 
 
 def workspace(nbytes: int, device, slot: str = "blas") -> torch.Tensor:
-    """A per-device, per-slot scratch buffer that only grows."""
-    key = (str(device), slot)
+    """A scratch buffer per (device, slot, stream) that only grows.
+
+    Keyed by the current CUDA stream so solves running concurrently on different
+    streams (the request server) never share scratch; work on one stream is
+    ordered, so reuse within a stream is safe."""
+    key = (str(device), slot, torch.cuda.current_stream(device).cuda_stream)
     buf = _WS.get(key)
     if buf is None or buf.numel() < nbytes:
         buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
         _WS[key] = buf
     return buf
+
+
+def release_workspaces(stream=None) -> None:
+    """Drop the scratch buffers of one stream (all streams when None)."""
+    sid = None if stream is None else stream.cuda_stream
+    for key in [k for k in _WS if sid is None or k[2] == sid]:
+        del _WS[key]
 
 
 def _c64(x: torch.Tensor) -> torch.Tensor:
@@ -55,10 +66,15 @@ def gram(A: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
         raise ValueError("gram: vector sizes differ")
     out = torch.empty((ma, mb), dtype=torch.complex128, device=A.device)
     from ._lib import load
+    from . import profiling
     nbytes = load().ef_gram_workspace_bytes(ma, mb, K)
     ws = workspace(nbytes, A.device, "gram")
+    tm = profiling.active()
+    ev = tm.begin() if tm is not None else None
     call("ef_gram", A.data_ptr(), B.data_ptr(), ma, mb, K, out.data_ptr(), ws.data_ptr(),
          ws.numel(), _stream())
+    if tm is not None:
+        tm.end("gram", ev, 8.0 * K * (ma + mb), 8.0 * ma * mb * K)
     return out
 
 
@@ -96,7 +112,12 @@ def rotate(C, S: torch.Tensor, out: torch.Tensor | None = None, mode: int = 0) -
         if mode != 0:
             raise ValueError("rotate: accumulate modes need an output")
         out = torch.empty((m_out,) + tuple(S.shape[1:]), dtype=torch.complex64, device=S.device)
+    from . import profiling
+    tm = profiling.active()
+    ev = tm.begin() if tm is not None else None
     call("ef_rotate", Cd.data_ptr(), S.data_ptr(), out.data_ptr(), m_in, m_out, K, mode, _stream())
+    if tm is not None:
+        tm.end("rotate", ev, 8.0 * K * (m_in + m_out * (1 if mode == 0 else 2)), 8.0 * m_in * m_out * K)
     return out
 
 

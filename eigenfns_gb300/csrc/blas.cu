@@ -91,14 +91,15 @@ __global__ void __launch_bounds__(GTHREADS) gram_kernel(const float2* __restrict
         }
     }
   }
-  double2* out = partial + (long long)blockIdx.z * ma * mb;
+  // partials are entry-major, (ma*mb, nsplit), so the reduction reads contiguous runs
 #pragma unroll
   for (int r = 0; r < 4; ++r)
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
       int i = i0 + ti + 8 * r, j = j0 + tj + 8 * c;
       if (i < ma && j < mb)
-        out[(long long)i * mb + j] = make_double2(dr[r][c] + (double)accr[r][c], di[r][c] + (double)acci[r][c]);
+        partial[((long long)i * mb + j) * gridDim.z + blockIdx.z] =
+            make_double2(dr[r][c] + (double)accr[r][c], di[r][c] + (double)acci[r][c]);
     }
 }
 
@@ -189,27 +190,36 @@ __global__ void __launch_bounds__(PG_THREADS) gram_pipe_kernel(const float2* __r
       }
     __syncthreads();
   }
-  double2* out = partial + (long long)blockIdx.z * ma * mb;
 #pragma unroll
   for (int r = 0; r < 2; ++r)
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
       int i = i0 + ti + 16 * r, j = j0 + tj + 8 * c;
-      if (i < ma && j < mb) out[(long long)i * mb + j] = make_double2((double)totr[r][c], (double)toti[r][c]);
+      if (i < ma && j < mb)
+        partial[((long long)i * mb + j) * gridDim.z + blockIdx.z] =
+            make_double2((double)totr[r][c], (double)toti[r][c]);
     }
 }
 
+// one warp per Gram entry: lanes stride the entry's contiguous split partials, then a
+// fixed shuffle tree (deterministic run to run)
 __global__ void gram_reduce_kernel(const double2* __restrict__ partial, int nsplit, int n,
                                    double2* __restrict__ G) {
-  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int e = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (e >= n) return;
+  const double2* p = partial + (long long)e * nsplit;
   double sr = 0.0, si = 0.0;
-  for (int s = 0; s < nsplit; ++s) {
-    double2 p = partial[(long long)s * n + e];
-    sr += p.x;
-    si += p.y;
+  for (int s = lane; s < nsplit; s += 32) {
+    double2 v = p[s];
+    sr += v.x;
+    si += v.y;
   }
-  G[e] = make_double2(sr, si);
+  for (int o = 16; o > 0; o >>= 1) {
+    sr += __shfl_down_sync(0xffffffffu, sr, o);
+    si += __shfl_down_sync(0xffffffffu, si, o);
+  }
+  if (lane == 0) G[e] = make_double2(sr, si);
 }
 
 int gram_splits(int ma, int mb, long long K) {
@@ -282,6 +292,106 @@ __global__ void __launch_bounds__(RTHREADS) rotate_kernel(const float2* __restri
         else if (mode > 0) { float2 v = *o; *o = make_float2(v.x + acc[ii].x, v.y + acc[ii].y); }
         else { float2 v = *o; *o = make_float2(v.x - acc[ii].x, v.y - acc[ii].y); }
       }
+    }
+  }
+}
+
+// Tiled variant for 16-byte aligned rows of even length and m_out <= 64 per CTA row:
+// a CTA owns 128 k-columns for up to 8*TI outputs; S rows (16 at a time) and the
+// matching C rows stream through two cp.async shared-memory stages; each thread keeps
+// a 4 (k) x TI (outputs) complex register tile, so every shared load feeds 8-16 FMAs.
+constexpr int RK_T = 256, RK_KT = 128, RK_JB = 16;
+
+template <int TI>
+__global__ void __launch_bounds__(RK_T) rotate_tiled_kernel(const float2* __restrict__ C,
+                                                            const float2* S, float2* out, int m_in,
+                                                            int m_out, long long K, int mode) {
+  constexpr int MO = 8 * TI;                            // outputs per CTA
+  __shared__ __align__(16) float2 Ss[2][RK_JB][RK_KT];  // 32 KB
+  __shared__ __align__(16) float2 Cs[2][RK_JB][MO];
+  const int tid = threadIdx.x, kg = tid & 31, ig = tid >> 5;
+  const long long k0 = (long long)blockIdx.x * RK_KT;
+  const int i0 = blockIdx.y * MO;
+  const int nst = (m_in + RK_JB - 1) / RK_JB;
+  auto issue = [&](int st, int buf) {
+    const int j0 = st * RK_JB;
+    // S: 16 rows x 128 complex = 1024 chunks of 16 B, 4 per thread
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+      const int e = tid + l * RK_T;
+      const int r = e >> 6, ch = e & 63;               // row, chunk of 2 complex
+      const long long k = k0 + 2 * ch;
+      const long long left = K - k;
+      int bytes = left >= 2 ? 16 : (left == 1 ? 8 : 0);
+      if (j0 + r >= m_in) bytes = 0;
+      const float2* g = S + (long long)(j0 + r < m_in ? j0 + r : 0) * K + (bytes ? k : 0);
+      unsigned sa = (unsigned)__cvta_generic_to_shared(&Ss[buf][r][2 * ch]);
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(g), "r"(bytes));
+    }
+    // C: 16 rows x MO complex; chunks of 2 complex
+    for (int e = tid; e < RK_JB * MO / 2; e += RK_T) {
+      const int r = e / (MO / 2), ch = e % (MO / 2);
+      const int i = i0 + 2 * ch;
+      int bytes = 0;
+      if (j0 + r < m_in && i < m_out) bytes = (i + 1 < m_out) ? 16 : 8;
+      const float2* g = C + (long long)(j0 + r < m_in ? j0 + r : 0) * m_out + (bytes ? i : 0);
+      unsigned sa = (unsigned)__cvta_generic_to_shared(&Cs[buf][r][2 * ch]);
+      // C rows are 8-byte aligned only: copy as two 8-byte pieces
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(sa), "l"(g), "r"(bytes >= 8 ? 8 : 0));
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(sa + 8), "l"(g + (bytes == 16 ? 1 : 0)),
+                   "r"(bytes == 16 ? 8 : 0));
+    }
+    asm volatile("cp.async.commit_group;\n" ::);
+  };
+  float2 acc[4][TI];
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int t = 0; t < TI; ++t) acc[q][t] = make_float2(0.f, 0.f);
+  issue(0, 0);
+  for (int st = 0; st < nst; ++st) {
+    const int buf = st & 1;
+    if (st + 1 < nst) {
+      issue(st + 1, buf ^ 1);
+      asm volatile("cp.async.wait_group 1;\n" ::);
+    } else {
+      asm volatile("cp.async.wait_group 0;\n" ::);
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int jj = 0; jj < RK_JB; ++jj) {
+      const float4 s01 = *reinterpret_cast<const float4*>(&Ss[buf][jj][4 * kg]);
+      const float4 s23 = *reinterpret_cast<const float4*>(&Ss[buf][jj][4 * kg + 2]);
+      const float2 sv[4] = {make_float2(s01.x, s01.y), make_float2(s01.z, s01.w),
+                            make_float2(s23.x, s23.y), make_float2(s23.z, s23.w)};
+#pragma unroll
+      for (int t2 = 0; t2 < TI; t2 += 2) {
+        const float4 cc = *reinterpret_cast<const float4*>(&Cs[buf][jj][ig * TI + t2]);
+        const float2 c0 = make_float2(cc.x, cc.y), c1 = make_float2(cc.z, cc.w);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          acc[q][t2].x = fmaf(c0.x, sv[q].x, fmaf(-c0.y, sv[q].y, acc[q][t2].x));
+          acc[q][t2].y = fmaf(c0.x, sv[q].y, fmaf(c0.y, sv[q].x, acc[q][t2].y));
+          acc[q][t2 + 1].x = fmaf(c1.x, sv[q].x, fmaf(-c1.y, sv[q].y, acc[q][t2 + 1].x));
+          acc[q][t2 + 1].y = fmaf(c1.x, sv[q].y, fmaf(c1.y, sv[q].x, acc[q][t2 + 1].y));
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // every S column of this CTA's k-range has been read: outputs may alias S when gridDim.y == 1
+#pragma unroll
+  for (int t = 0; t < TI; ++t) {
+    const int i = i0 + ig * TI + t;
+    if (i >= m_out) continue;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const long long k = k0 + 4 * kg + q;
+      if (k >= K) continue;
+      float2* o = out + (long long)i * K + k;
+      if (mode == 0) *o = acc[q][t];
+      else if (mode > 0) { float2 v = *o; *o = make_float2(v.x + acc[q][t].x, v.y + acc[q][t].y); }
+      else { float2 v = *o; *o = make_float2(v.x - acc[q][t].x, v.y - acc[q][t].y); }
     }
   }
 }
@@ -607,7 +717,7 @@ int ef_gram(const float* A, const float* B, int ma, int mb, long long K, double*
                                           (double2*)work);
   int n = ma * mb;
   ef_count_launches(1);
-  gram_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>((const double2*)work, ns, n, (double2*)G);
+  gram_reduce_kernel<<<(n + 7) / 8, 256, 0, st>>>((const double2*)work, ns, n, (double2*)G);
   return ef_check_launch();
 }
 
@@ -637,7 +747,7 @@ int ef_gram_noalloc(const float* A, const float* B, int ma, int mb, long long K,
     gram_kernel<<<grid, GTHREADS, 0, st>>>((const float2*)A, (const float2*)B, ma, mb, K, kchunk,
                                           (double2*)scratch);
   int n = ma * mb;
-  gram_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>((const double2*)scratch, ns, n, (double2*)G);
+  gram_reduce_kernel<<<(n + 7) / 8, 256, 0, st>>>((const double2*)scratch, ns, n, (double2*)G);
   return ef_check_launch();
 }
 
@@ -645,17 +755,30 @@ int ef_rotate(const float* C, const float* S, float* out, int m_in, int m_out, l
               void* stream) {
   if (!C || !S || !out || m_in <= 0 || m_out <= 0 || K <= 0) return ef_fail(EF_ERR_INVALID, "bad rotate arguments");
   if ((size_t)m_in * RT * sizeof(float2) > 200 * 1024) return ef_fail(EF_ERR_TOO_LARGE, "m_in too large for rotate");
-  int ty = (m_out + RT - 1) / RT;
+  const bool tiled = (K % 2 == 0) && ((((uintptr_t)S) | ((uintptr_t)out)) % 16 == 0);
+  const int TIc = m_out <= 16 ? 2 : (m_out <= 32 ? 4 : 8);
+  int ty = tiled ? (m_out + 8 * TIc - 1) / (8 * TIc) : (m_out + RT - 1) / RT;
   const char* s0 = (const char*)S;
   const char* s1 = s0 + (size_t)m_in * K * sizeof(float2);
   const char* o0 = (const char*)out;
   const char* o1 = o0 + (size_t)m_out * K * sizeof(float2);
   bool overlap = (o0 < s1) && (s0 < o1);
-  if (overlap && !(o0 == s0 && ty == 1))
+  if (overlap && !(o0 == s0 && m_out <= 32 && ty == 1))
     return ef_fail(EF_ERR_INVALID, "rotate: out may alias S only exactly and with m_out <= 32");
   cudaStream_t st = (cudaStream_t)stream;
+  if (tiled) {
+    dim3 g((unsigned)((K + RK_KT - 1) / RK_KT), ty);
+    ef_count_launches(1);
+    if (TIc == 2)
+      rotate_tiled_kernel<2><<<g, RK_T, 0, st>>>((const float2*)C, (const float2*)S, (float2*)out, m_in, m_out, K, mode);
+    else if (TIc == 4)
+      rotate_tiled_kernel<4><<<g, RK_T, 0, st>>>((const float2*)C, (const float2*)S, (float2*)out, m_in, m_out, K, mode);
+    else
+      rotate_tiled_kernel<8><<<g, RK_T, 0, st>>>((const float2*)C, (const float2*)S, (float2*)out, m_in, m_out, K, mode);
+    return ef_check_launch();
+  }
   size_t smem = (size_t)m_in * RT * sizeof(float2);
-  if (smem > 48 * 1024) cudaFuncSetAttribute(rotate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  set_smem_once(rotate_kernel, smem);
   long long bx = (K + RTHREADS - 1) / RTHREADS;
   long long cap = (152 * 8 + ty - 1) / ty;
   if (bx > cap) bx = cap;

@@ -6,6 +6,10 @@
 #include "status.h"
 
 #include <atomic>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
 
 namespace {
 thread_local std::string g_last_error;
@@ -13,6 +17,32 @@ std::atomic<unsigned long long> g_launches{0};
 }
 
 void ef_count_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
+
+namespace {
+struct SmemEntry {
+  const void* kernel;
+  int device;
+  size_t bytes;
+};
+std::mutex g_smem_mu;
+std::vector<SmemEntry> g_smem;
+}  // namespace
+
+void ef::set_smem_limit(const void* kernel, size_t smem) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(g_smem_mu);
+  for (SmemEntry& e : g_smem) {
+    if (e.kernel == kernel && e.device == dev) {
+      if (e.bytes >= smem) return;
+      if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess)
+        e.bytes = smem;
+      return;
+    }
+  }
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess)
+    g_smem.push_back({kernel, dev, smem});
+}
 
 int ef_fail(int code, const char* msg) {
   g_last_error = msg ? msg : "";

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+
 #include "../../include/eigenfns_gb300.h"
 
 namespace ef {
@@ -39,19 +40,22 @@ __device__ __forceinline__ Frame make_frame(float Kx, float Ky, float Kz, bool s
   float ax, ay, az;
   if (!sw) { ax = Ky; ay = -Kx; az = 0.f; }       // K x z
   else     { ax = 0.f; ay = Kz; az = -Ky; }       // K x x
-  float n1 = sqrtf(ax * ax + ay * ay + az * az);
-  if (n1 == 0.f) {
+  float n1sq = ax * ax + ay * ay + az * az;
+  if (n1sq == 0.f) {
     f.t1x = f.t1y = f.t1z = f.t2x = f.t2y = f.t2z = 0.f;
     return f;
   }
-  ax /= n1; ay /= n1; az /= n1;
+  // normalise with one reciprocal square root each (a few ulp, like the fp64
+  // frame rounded to fp32)
+  const float r1 = rsqrtf(n1sq);
+  ax *= r1; ay *= r1; az *= r1;
   float bx = Ky * az - Kz * ay;
   float by = Kz * ax - Kx * az;
   float bz = Kx * ay - Ky * ax;
-  float n2 = sqrtf(bx * bx + by * by + bz * bz);
-  if (n2 == 0.f) n2 = 1.f;
+  float n2sq = bx * bx + by * by + bz * bz;
+  const float r2 = n2sq > 0.f ? rsqrtf(n2sq) : 1.f;
   f.t1x = ax; f.t1y = ay; f.t1z = az;
-  f.t2x = bx / n2; f.t2y = by / n2; f.t2z = bz / n2;
+  f.t2x = bx * r2; f.t2y = by * r2; f.t2z = bz * r2;
   return f;
 }
 
@@ -61,6 +65,16 @@ __device__ __forceinline__ Frame frame_at(const float* __restrict__ kax,
   long long idx = ((long long)x * G + y) * G + z;
   bool sw = (swap[idx >> 5] >> (idx & 31)) & 1u;
   return make_frame(kax[x], kax[G + y], kax[2 * G + z], sw);
+}
+
+// Raise a kernel's dynamic shared-memory limit once per (kernel, device), and
+// again only for a larger size: the attribute call costs far more than a launch,
+// and the pipeline launches its kernels hundreds of times per solve.
+void set_smem_limit(const void* kernel, size_t smem);
+
+template <class K>
+inline void set_smem_once(K kernel, size_t smem) {
+  if (smem > 48 * 1024) set_smem_limit(reinterpret_cast<const void*>(kernel), smem);
 }
 
 }  // namespace ef

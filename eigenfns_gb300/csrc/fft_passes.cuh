@@ -42,10 +42,20 @@ struct Geo {
     return c;
   }
   static constexpr int NR = nr_pick();
-  // y/x-pass z-columns per tile: largest divisor of G not above 16
+  // z-pass rows per tile: pass A (this split R1 <= R2) runs NRA*R2 items in its first
+  // step, pass E (R1 >= R2) runs NRE*R1 in its second; both stay within 256 items
+  // and 64 KB of exchange buffer
+  static constexpr int nrz_pick(int per_row) {
+    int c = 256 / per_row > 0 ? 256 / per_row : 1;
+    while (c > 1 && (((G * G) % c) != 0 || 3 * c * PS * 8 > 64 * 1024)) --c;
+    return c;
+  }
+  static constexpr int NRA = nrz_pick(R2_);
+  static constexpr int NRE = nrz_pick(R1_);
+  // y/x-pass z-columns per tile: largest divisor of G not above 32
   static constexpr int nz_pick() {
-    int c = G < 16 ? G : 16;
-    while (c > 1 && G % c != 0) --c;
+    int c = G < 32 ? G : 32;
+    while (c > 1 && (G % c != 0 || 2 * c * PS * 8 > 80 * 1024)) --c;
     return c;
   }
   static constexpr int NZ = nz_pick();
@@ -144,58 +154,73 @@ __device__ __forceinline__ void step2_load(const float2* exch, int q, int k1, fl
 }
 
 // ---------------------------------------------------------------------------------
-// Pass A: z-pencils, inverse, with the transverse -> Cartesian build.
-// grid (G*G/NR, mb); X points at the sub-batch's first vector.
+// Pass A: z-pencils, inverse, with the transverse -> Cartesian build. GEO is the
+// split with the small factor first (R1 <= R2): a first-step item owns voxels
+// z = t2 + R2*n1 of one row, loads (a, b), computes the frame once per voxel and
+// transforms all 3 Cartesian components in registers.
+// grid (G*G/NRA, mb); X points at the sub-batch's first vector.
 template <class GEO, int BUILD>
 __global__ void __launch_bounds__(kThreads) pass_a_kernel(PassArgs a) {
-  constexpr int G = GEO::G, NR = GEO::NR, NP = 3 * NR;
+  constexpr int G = GEO::G, NR = GEO::NRA, NP = 3 * NR, R1 = GEO::R1, R2 = GEO::R2;
   extern __shared__ float2 smem[];
-  float2* nat = smem;
-  float2* exch = smem + NP * GEO::PS;
+  float2* exch = smem;
   float2* tw_s = exch + NP * GEO::PS;
   load_twiddles<GEO>(tw_s, a.tw);
+  __syncthreads();
   const long long N = (long long)G * G * G;
   const int v = blockIdx.y;
   const int row0 = blockIdx.x * NR;
   const float2* Xa = a.X + (long long)v * 2 * N;
   const float2* Xb = Xa + N;
-  for (int e = threadIdx.x; e < NR * G; e += blockDim.x) {
-    int r = e / G, z = e % G;
-    int row = row0 + r, x = row / G, y = row % G;
-    long long idx = (long long)row * G + z;
-    Frame f = frame_at(a.kax, a.swap, G, x, y, z);
-    float2 av = Xa[idx], bv = Xb[idx];
-    float2 c1, c2;
-    if (BUILD == BUILD_THETA) {           // c1 = -i kn b, c2 = i kn a
-      c1 = make_float2(f.kn * bv.y, -f.kn * bv.x);
-      c2 = make_float2(-f.kn * av.y, f.kn * av.x);
-    } else if (BUILD == BUILD_PRECOND) {  // c1 = i b / knr, c2 = -i a / knr
-      float knr = fmaxf(f.kn, a.kn_floor);
-      c1 = make_float2(-bv.y / knr, bv.x / knr);
-      c2 = make_float2(av.y / knr, -av.x / knr);
-    } else {                               // Cartesian H: a t1 + b t2
-      c1 = av;
-      c2 = bv;
+  for (int it = threadIdx.x; it < NR * R2; it += blockDim.x) {
+    const int r = it / R2, t2 = it % R2;
+    const int row = row0 + r, x = row / G, y = row % G;
+    float2 cx[R1], cy[R1], cz[R1];
+#pragma unroll
+    for (int n1 = 0; n1 < R1; ++n1) {
+      const int z = t2 + R2 * n1;
+      const long long idx = (long long)row * G + z;
+      const Frame f = frame_at(a.kax, a.swap, G, x, y, z);
+      const float2 av = Xa[idx], bv = Xb[idx];
+      float2 c1, c2;
+      if (BUILD == BUILD_THETA) {           // c1 = -i kn b, c2 = i kn a
+        c1 = make_float2(f.kn * bv.y, -f.kn * bv.x);
+        c2 = make_float2(-f.kn * av.y, f.kn * av.x);
+      } else if (BUILD == BUILD_PRECOND) {  // c1 = i b / knr, c2 = -i a / knr
+        const float ik = 1.0f / fmaxf(f.kn, a.kn_floor);
+        c1 = make_float2(-bv.y * ik, bv.x * ik);
+        c2 = make_float2(av.y * ik, -av.x * ik);
+      } else {                               // Cartesian H: a t1 + b t2
+        c1 = av;
+        c2 = bv;
+      }
+      cx[n1] = make_float2(c1.x * f.t1x + c2.x * f.t2x, c1.y * f.t1x + c2.y * f.t2x);
+      cy[n1] = make_float2(c1.x * f.t1y + c2.x * f.t2y, c1.y * f.t1y + c2.y * f.t2y);
+      cz[n1] = make_float2(c1.x * f.t1z + c2.x * f.t2z, c1.y * f.t1z + c2.y * f.t2z);
     }
-    nat[(0 * NR + r) * GEO::PS + z] = make_float2(c1.x * f.t1x + c2.x * f.t2x, c1.y * f.t1x + c2.y * f.t2x);
-    nat[(1 * NR + r) * GEO::PS + z] = make_float2(c1.x * f.t1y + c2.x * f.t2y, c1.y * f.t1y + c2.y * f.t2y);
-    nat[(2 * NR + r) * GEO::PS + z] = make_float2(c1.x * f.t1z + c2.x * f.t2z, c1.y * f.t1z + c2.y * f.t2z);
-  }
-  __syncthreads();
-  for (int it = threadIdx.x; it < NP * GEO::R2; it += blockDim.x) {
-    int q = it / GEO::R2, t2 = it % GEO::R2;
-    step1_smem<GEO, +1>(nat, exch, tw_s, q, t2);
+    DFT<R1, +1>::run(cx);
+    DFT<R1, +1>::run(cy);
+    DFT<R1, +1>::run(cz);
+#pragma unroll
+    for (int k1 = 0; k1 < R1; ++k1) {
+      float2 tw = make_float2(1.f, 0.f);
+      if (k1 != 0 && t2 != 0) tw = tw_get<+1>(tw_s, t2 * k1);
+      const int o = k1 * GEO::XS + t2;
+      exch[(0 * NR + r) * GEO::PS + o] = (k1 && t2) ? cmul(cx[k1], tw) : cx[k1];
+      exch[(1 * NR + r) * GEO::PS + o] = (k1 && t2) ? cmul(cy[k1], tw) : cy[k1];
+      exch[(2 * NR + r) * GEO::PS + o] = (k1 && t2) ? cmul(cz[k1], tw) : cz[k1];
+    }
   }
   __syncthreads();
   float2* E = a.E + (long long)v * 3 * N;
-  for (int it = threadIdx.x; it < NP * GEO::R1; it += blockDim.x) {
-    int q = it / GEO::R1, k1 = it % GEO::R1;
-    float2 u[GEO::R2];
+  for (int it = threadIdx.x; it < NP * R1; it += blockDim.x) {
+    const int q = it / R1, k1 = it % R1;
+    float2 u[R2];
     step2_load<GEO, +1>(exch, q, k1, u);
-    int j = q / NR, r = q % NR;
+    const int j = q / NR, r = q % NR;
     float2* dst = E + (long long)j * N + (long long)(row0 + r) * G;
 #pragma unroll
-    for (int k2 = 0; k2 < GEO::R2; ++k2) dst[k1 + GEO::R1 * k2] = u[k2];
+    for (int k2 = 0; k2 < R2; ++k2) dst[k1 + R1 * k2] = u[k2];
   }
 }
 
@@ -298,12 +323,16 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
   return s;
 }
 
+// Pass E: z-pencils, forward, then projection, curl and the epilogue. GEO is the
+// split with the large factor first (R1 >= R2): a second-step item owns outputs
+// z = k1 + R1*k2 of one row for all 3 components, so the frame is computed once
+// per voxel and the projection happens in registers.
+// grid (G*G/NRE, mb); per-vector pointers (out, X, T0, Y, Z) at the sub-batch start.
 template <class GEO, int EPI>
 __global__ void __launch_bounds__(kThreads) pass_e_kernel(PassArgs a) {
-  constexpr int G = GEO::G, NR = GEO::NR, NP = 3 * NR;
+  constexpr int G = GEO::G, NR = GEO::NRE, NP = 3 * NR, R1 = GEO::R1, R2 = GEO::R2;
   extern __shared__ float2 smem[];
-  float2* nat = smem;
-  float2* exch = smem + NP * GEO::PS;
+  float2* exch = smem;
   float2* tw_s = exch + NP * GEO::PS;
   __shared__ double red[kThreads / 32];
   load_twiddles<GEO>(tw_s, a.tw);
@@ -312,82 +341,83 @@ __global__ void __launch_bounds__(kThreads) pass_e_kernel(PassArgs a) {
   const int v = blockIdx.y;
   const int row0 = blockIdx.x * NR;
   const float2* E = a.E + (long long)v * 3 * N;
-  for (int it = threadIdx.x; it < NP * GEO::R2; it += blockDim.x) {
-    int q = it / GEO::R2, t2 = it % GEO::R2;
-    int j = q / NR, r = q % NR;
+  for (int it = threadIdx.x; it < NP * R2; it += blockDim.x) {
+    const int q = it / R2, t2 = it % R2;
+    const int j = q / NR, r = q % NR;
     step1_global<GEO, -1>(E, (long long)j * N + (long long)(row0 + r) * G, 1, exch, tw_s, q, t2);
-  }
-  __syncthreads();
-  for (int it = threadIdx.x; it < NP * GEO::R1; it += blockDim.x) {
-    int q = it / GEO::R1, k1 = it % GEO::R1;
-    float2 u[GEO::R2];
-    step2_load<GEO, -1>(exch, q, k1, u);
-#pragma unroll
-    for (int k2 = 0; k2 < GEO::R2; ++k2) nat[q * GEO::PS + k1 + GEO::R1 * k2] = u[k2];
   }
   __syncthreads();
   const long long vo = (long long)v * 2 * N;
   double acc0 = 0.0, acc1 = 0.0;
-  for (int e = threadIdx.x; e < NR * G; e += blockDim.x) {
-    int r = e / G, z = e % G;
-    int row = row0 + r, x = row / G, y = row % G;
-    long long idx = (long long)row * G + z;
-    Frame f = frame_at(a.kax, a.swap, G, x, y, z);
-    float2 dx = nat[(0 * NR + r) * GEO::PS + z];
-    float2 dy = nat[(1 * NR + r) * GEO::PS + z];
-    float2 dz = nat[(2 * NR + r) * GEO::PS + z];
-    float2 f1 = make_float2(f.t1x * dx.x + f.t1y * dy.x + f.t1z * dz.x, f.t1x * dx.y + f.t1y * dy.y + f.t1z * dz.y);
-    float2 f2 = make_float2(f.t2x * dx.x + f.t2y * dy.x + f.t2z * dz.x, f.t2x * dx.y + f.t2y * dy.y + f.t2z * dz.y);
-    float2 o0, o1;
-    if (EPI == EPI_PRECOND) {
-      float knr = fmaxf(f.kn, a.kn_floor);
-      o0 = make_float2(-f2.y / knr, f2.x / knr);   // i f2 / knr
-      o1 = make_float2(f1.y / knr, -f1.x / knr);   // -i f1 / knr
-    } else {
-      o0 = make_float2(f.kn * f2.y, -f.kn * f2.x); // -i kn f2
-      o1 = make_float2(-f.kn * f1.y, f.kn * f1.x); //  i kn f1
-    }
-    if (EPI == EPI_THETA || EPI == EPI_PRECOND) {
-      a.out[vo + idx] = o0;
-      a.out[vo + N + idx] = o1;
-    } else {
-      // B T1 = s Θ T1 - T1 with T1 the operator input
-      float2 t1a = a.X[vo + idx], t1b = a.X[vo + N + idx];
-      float2 b0 = make_float2(a.s * o0.x - t1a.x, a.s * o0.y - t1a.y);
-      float2 b1 = make_float2(a.s * o1.x - t1b.x, a.s * o1.y - t1b.y);
-      if (EPI == EPI_CHEB_FIRST) {
-        a.out[vo + idx] = b0;
-        a.out[vo + N + idx] = b1;
-        a.Y[vo + idx] = make_float2(a.c0 * t1a.x + a.c1 * b0.x, a.c0 * t1a.y + a.c1 * b0.y);
-        a.Y[vo + N + idx] = make_float2(a.c0 * t1b.x + a.c1 * b1.x, a.c0 * t1b.y + a.c1 * b1.y);
-      } else if (EPI == EPI_KPM_FIRST || EPI == EPI_KPM_COUNT_FIRST) {
-        a.out[vo + idx] = b0;
-        a.out[vo + N + idx] = b1;
-        acc0 += (double)(t1a.x * t1a.x + t1a.y * t1a.y + t1b.x * t1b.x + t1b.y * t1b.y);
-        acc1 += (double)(t1a.x * b0.x + t1a.y * b0.y + t1b.x * b1.x + t1b.y * b1.y);
+  for (int it = threadIdx.x; it < NR * R1; it += blockDim.x) {
+    const int r = it / R1, k1 = it % R1;
+    const int row = row0 + r, x = row / G, y = row % G;
+    float2 dx[R2], dy[R2], dz[R2];
+    step2_load<GEO, -1>(exch, 0 * NR + r, k1, dx);
+    step2_load<GEO, -1>(exch, 1 * NR + r, k1, dy);
+    step2_load<GEO, -1>(exch, 2 * NR + r, k1, dz);
+    float f0 = 0.f, f1acc = 0.f;
+#pragma unroll
+    for (int k2 = 0; k2 < R2; ++k2) {
+      const int z = k1 + R1 * k2;
+      const long long idx = (long long)row * G + z;
+      const Frame f = frame_at(a.kax, a.swap, G, x, y, z);
+      const float2 f1 = make_float2(f.t1x * dx[k2].x + f.t1y * dy[k2].x + f.t1z * dz[k2].x,
+                                    f.t1x * dx[k2].y + f.t1y * dy[k2].y + f.t1z * dz[k2].y);
+      const float2 f2 = make_float2(f.t2x * dx[k2].x + f.t2y * dy[k2].x + f.t2z * dz[k2].x,
+                                    f.t2x * dx[k2].y + f.t2y * dy[k2].y + f.t2z * dz[k2].y);
+      float2 o0, o1;
+      if (EPI == EPI_PRECOND) {
+        const float ik = 1.0f / fmaxf(f.kn, a.kn_floor);
+        o0 = make_float2(-f2.y * ik, f2.x * ik);   // i f2 / knr
+        o1 = make_float2(f1.y * ik, -f1.x * ik);   // -i f1 / knr
       } else {
-        float2 p0 = a.T0[vo + idx], p1 = a.T0[vo + N + idx];
-        float2 n0 = make_float2(2.f * b0.x - p0.x, 2.f * b0.y - p0.y);
-        float2 n1 = make_float2(2.f * b1.x - p1.x, 2.f * b1.y - p1.y);
-        a.T0[vo + idx] = n0;
-        a.T0[vo + N + idx] = n1;
-        if (EPI == EPI_CHEB) {
-          float2 y0 = a.Y[vo + idx], y1 = a.Y[vo + N + idx];
-          a.Y[vo + idx] = make_float2(fmaf(a.c1, n0.x, y0.x), fmaf(a.c1, n0.y, y0.y));
-          a.Y[vo + N + idx] = make_float2(fmaf(a.c1, n1.x, y1.x), fmaf(a.c1, n1.y, y1.y));
-        } else if (EPI == EPI_KPM) {
-          acc0 += (double)(t1a.x * t1a.x + t1a.y * t1a.y + t1b.x * t1b.x + t1b.y * t1b.y);
-          acc1 += (double)(n0.x * t1a.x + n0.y * t1a.y + n1.x * t1b.x + n1.y * t1b.y);
-        } else {  // EPI_KPM_COUNT: <Z, T2>
-          float2 z0 = a.Z[vo + idx], z1 = a.Z[vo + N + idx];
-          acc0 += (double)(z0.x * n0.x + z0.y * n0.y + z1.x * n1.x + z1.y * n1.y);
+        o0 = make_float2(f.kn * f2.y, -f.kn * f2.x); // -i kn f2
+        o1 = make_float2(-f.kn * f1.y, f.kn * f1.x); //  i kn f1
+      }
+      if (EPI == EPI_THETA || EPI == EPI_PRECOND) {
+        a.out[vo + idx] = o0;
+        a.out[vo + N + idx] = o1;
+      } else {
+        const float2 t1a = a.X[vo + idx], t1b = a.X[vo + N + idx];
+        const float2 b0 = make_float2(a.s * o0.x - t1a.x, a.s * o0.y - t1a.y);
+        const float2 b1 = make_float2(a.s * o1.x - t1b.x, a.s * o1.y - t1b.y);
+        if (EPI == EPI_CHEB_FIRST) {
+          a.out[vo + idx] = b0;
+          a.out[vo + N + idx] = b1;
+          a.Y[vo + idx] = make_float2(a.c0 * t1a.x + a.c1 * b0.x, a.c0 * t1a.y + a.c1 * b0.y);
+          a.Y[vo + N + idx] = make_float2(a.c0 * t1b.x + a.c1 * b1.x, a.c0 * t1b.y + a.c1 * b1.y);
+        } else if (EPI == EPI_KPM_FIRST || EPI == EPI_KPM_COUNT_FIRST) {
+          a.out[vo + idx] = b0;
+          a.out[vo + N + idx] = b1;
+          f0 += t1a.x * t1a.x + t1a.y * t1a.y + t1b.x * t1b.x + t1b.y * t1b.y;
+          f1acc += t1a.x * b0.x + t1a.y * b0.y + t1b.x * b1.x + t1b.y * b1.y;
+        } else {
+          const float2 p0 = a.T0[vo + idx], p1 = a.T0[vo + N + idx];
+          const float2 n0 = make_float2(2.f * b0.x - p0.x, 2.f * b0.y - p0.y);
+          const float2 n1 = make_float2(2.f * b1.x - p1.x, 2.f * b1.y - p1.y);
+          a.T0[vo + idx] = n0;
+          a.T0[vo + N + idx] = n1;
+          if (EPI == EPI_CHEB) {
+            const float2 y0 = a.Y[vo + idx], y1 = a.Y[vo + N + idx];
+            a.Y[vo + idx] = make_float2(fmaf(a.c1, n0.x, y0.x), fmaf(a.c1, n0.y, y0.y));
+            a.Y[vo + N + idx] = make_float2(fmaf(a.c1, n1.x, y1.x), fmaf(a.c1, n1.y, y1.y));
+          } else if (EPI == EPI_KPM) {
+            f0 += t1a.x * t1a.x + t1a.y * t1a.y + t1b.x * t1b.x + t1b.y * t1b.y;
+            f1acc += n0.x * t1a.x + n0.y * t1a.y + n1.x * t1b.x + n1.y * t1b.y;
+          } else {  // EPI_KPM_COUNT: <Z, T2>
+            const float2 z0 = a.Z[vo + idx], z1 = a.Z[vo + N + idx];
+            f0 += z0.x * n0.x + z0.y * n0.y + z1.x * n1.x + z1.y * n1.y;
+          }
         }
       }
     }
+    acc0 += (double)f0;
+    acc1 += (double)f1acc;
   }
   if (EPI >= EPI_KPM) {
-    double s0 = block_sum(acc0, red);
-    double s1 = block_sum(acc1, red);
+    const double s0 = block_sum(acc0, red);
+    const double s1 = block_sum(acc1, red);
     if (threadIdx.x == 0) {
       double* p = a.partials + ((long long)v * gridDim.x + blockIdx.x) * 2;
       p[0] = s0;

@@ -127,7 +127,8 @@ size_t subbatch_cap_bytes() {
 
 struct Sizes {
   long long N;
-  int tiles;
+  int tiles;           // pass-E tiles per vector (one partial each)
+  int tiles_a;         // pass-A tiles per vector
   size_t per_vec;      // E bytes per vector
   size_t per_vec_part; // partial bytes per vector
 };
@@ -135,7 +136,8 @@ struct Sizes {
 Sizes sizes_of(const ef_op* op, const Plan* p) {
   Sizes s;
   s.N = op->N;
-  s.tiles = (op->G * op->G) / p->NR;
+  s.tiles = (op->G * op->G) / p->NRE;
+  s.tiles_a = (op->G * op->G) / p->NRA;
   s.per_vec = (size_t)3 * s.N * sizeof(float2);
   s.per_vec_part = ((size_t)s.tiles * 2 * sizeof(double) + 255) / 256 * 256;
   return s;
@@ -171,8 +173,9 @@ int run_pipe(const ef_op* op, const Pipe& pp, const float2* X, float2* out, floa
   float2* E = reinterpret_cast<float2*>(work);
   size_t e_bytes = (size_t)mb * sz.per_vec;
   double* partials = reinterpret_cast<double*>(reinterpret_cast<char*>(work) + (e_bytes + 255) / 256 * 256);
-  const int G = op->G, NR = p->NR, NZ = p->NZ, PS = p->PS;
-  const size_t smem_ae = (size_t)(2 * 3 * NR * PS + G) * sizeof(float2);
+  const int G = op->G, NZ = p->NZ, PS = p->PS;
+  const size_t smem_a = (size_t)(3 * p->NRA * p->PSA + G) * sizeof(float2);
+  const size_t smem_e = (size_t)(3 * p->NRE * p->PSE + G) * sizeof(float2);
   const size_t smem_y = (size_t)(NZ * PS + G) * sizeof(float2);
   const size_t smem_c = (size_t)(2 * NZ * PS + G) * sizeof(float2);
   const long long N2 = 2 * op->N;
@@ -197,11 +200,11 @@ int run_pipe(const ef_op* op, const Pipe& pp, const float2* X, float2* out, floa
     a.c0 = c0;
     a.c1 = c1;
     a.G = G;
-    p->a[pp.build](dim3(sz.tiles, nb), smem_ae, st, a);
+    p->a[pp.build](dim3(sz.tiles_a, nb), smem_a, st, a);
     p->y[0](dim3(G / NZ, G, 3 * nb), smem_y, st, a);
     p->c[pp.wmode](dim3(G / NZ, G, 3 * nb), smem_c, st, a);
     p->y[1](dim3(G / NZ, G, 3 * nb), smem_y, st, a);
-    p->e[pp.epi](dim3(sz.tiles, nb), smem_ae, st, a);
+    p->e[pp.epi](dim3(sz.tiles, nb), smem_e, st, a);
     if (pp.fin >= 0) {
       double* o = (pp.fin == FIN_COUNT_FIRST || pp.fin == FIN_COUNT_STEP) ? fin_out + v0 : fin_out + (long long)v0 * fin_ld;
       ef_count_launches(1);
@@ -367,7 +370,7 @@ static int realspace(const ef_op* op, const float* X, float* out, const float* v
   if (!op || !X || !out || m <= 0) return ef_fail(EF_ERR_INVALID, "null argument or m <= 0");
   const Plan* p = find_plan(op->G);
   if (!p) return ef_fail(EF_ERR_UNSUPPORTED, "no FFT plan for this grid");
-  const int G = op->G, NR = p->NR, NZ = p->NZ, PS = p->PS;
+  const int G = op->G, NZ = p->NZ, PS = p->PS;
   PassArgs a;
   std::memset(&a, 0, sizeof(a));
   a.X = (const float2*)X;
@@ -380,8 +383,8 @@ static int realspace(const ef_op* op, const float* X, float* out, const float* v
   a.inv_n = 1.0f / (float)op->N;
   a.kn_floor = op->kn_floor;
   a.G = G;
-  const int tiles = G * G / NR;
-  p->a[build](dim3(tiles, m), (size_t)(2 * 3 * NR * PS + G) * sizeof(float2), st, a);
+  const int tiles = G * G / p->NRA;
+  p->a[build](dim3(tiles, m), (size_t)(3 * p->NRA * p->PSA + G) * sizeof(float2), st, a);
   p->y[0](dim3(G / NZ, G, 3 * m), (size_t)(NZ * PS + G) * sizeof(float2), st, a);
   p->c[wmode](dim3(G / NZ, G, 3 * m), (size_t)(2 * NZ * PS + G) * sizeof(float2), st, a);
   return ef_check_launch();

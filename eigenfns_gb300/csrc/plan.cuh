@@ -2,6 +2,7 @@
 // for its split G = R1 * R2. Plans are instantiated in plans_*.cu so the
 // translation units compile in parallel.
 #pragma once
+#include <atomic>
 #include <vector>
 
 #include "fft_passes.cuh"
@@ -12,7 +13,9 @@ namespace ef {
 using Launch = void (*)(dim3, size_t, cudaStream_t, const PassArgs&);
 
 struct Plan {
-  int G, R1, R2, NR, NZ, PS;
+  int G, R1, R2, NZ, PS;   // y/x passes: split R1 >= R2, NZ z-columns per tile
+  int NRA, PSA;            // pass A: split (R2, R1), NRA rows per tile
+  int NRE, PSE;            // pass E: split (R1, R2), NRE rows per tile
   Launch a[3];       // BuildMode
   Launch y[2];       // 0 inverse, 1 forward
   Launch c[4];       // WMode
@@ -21,7 +24,7 @@ struct Plan {
 
 template <class K>
 void set_smem(K kernel, size_t smem) {
-  if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  set_smem_once(kernel, smem);
 }
 
 template <class GEO, int B>
@@ -49,20 +52,28 @@ void launch_e(dim3 g, size_t s, cudaStream_t st, const PassArgs& a) {
   pass_e_kernel<GEO, E><<<g, kThreads, s, st>>>(a);
 }
 
-template <int R1, int R2>
+// y/x passes use the split (R1, R2); pass A uses (RA1, RA2) with the small factor
+// first (the 3 components of RA1 voxels live in registers), pass E uses (RE1, RE2)
+// with the small factor last (the 3 components of RE2 outputs live in registers).
+template <int R1, int R2, int RA1 = R2, int RA2 = R1, int RE1 = R1, int RE2 = R2>
 Plan make_plan() {
-  using GE = Geo<R1, R2>;
+  using GY = Geo<R1, R2>;
+  using GA = Geo<RA1, RA2>;
+  using GE = Geo<RE1, RE2>;
+  static_assert(GA::G == GY::G && GE::G == GY::G, "splits of one grid edge");
   Plan p;
-  p.G = GE::G; p.R1 = R1; p.R2 = R2; p.NR = GE::NR; p.NZ = GE::NZ; p.PS = GE::PS;
-  p.a[0] = launch_a<GE, BUILD_THETA>;
-  p.a[1] = launch_a<GE, BUILD_PRECOND>;
-  p.a[2] = launch_a<GE, BUILD_CART>;
-  p.y[0] = launch_y<GE, +1>;
-  p.y[1] = launch_y<GE, -1>;
-  p.c[0] = launch_c<GE, W_INV_EPS>;
-  p.c[1] = launch_c<GE, W_EPS>;
-  p.c[2] = launch_c<GE, W_INV_ONLY>;
-  p.c[3] = launch_c<GE, W_INV_ONLY_EPS>;
+  p.G = GY::G; p.R1 = R1; p.R2 = R2; p.NZ = GY::NZ; p.PS = GY::PS;
+  p.NRA = GA::NRA; p.PSA = GA::PS;
+  p.NRE = GE::NRE; p.PSE = GE::PS;
+  p.a[0] = launch_a<GA, BUILD_THETA>;
+  p.a[1] = launch_a<GA, BUILD_PRECOND>;
+  p.a[2] = launch_a<GA, BUILD_CART>;
+  p.y[0] = launch_y<GY, +1>;
+  p.y[1] = launch_y<GY, -1>;
+  p.c[0] = launch_c<GY, W_INV_EPS>;
+  p.c[1] = launch_c<GY, W_EPS>;
+  p.c[2] = launch_c<GY, W_INV_ONLY>;
+  p.c[3] = launch_c<GY, W_INV_ONLY_EPS>;
   p.e[0] = launch_e<GE, EPI_THETA>;
   p.e[1] = launch_e<GE, EPI_PRECOND>;
   p.e[2] = launch_e<GE, EPI_CHEB>;

@@ -5,8 +5,8 @@ namespace ef {
 
 void add_plans_large(std::vector<Plan>& v) {
   v.push_back(make_plan<16, 8>());   // G = 128
-  v.push_back(make_plan<16, 12>());   // G = 192
-  v.push_back(make_plan<16, 16>());   // G = 256
+  v.push_back(make_plan<16, 12, 8, 24, 24, 8>());   // G = 192
+  v.push_back(make_plan<16, 16, 8, 32, 32, 8>());   // G = 256
 }
 
 }  // namespace ef

@@ -127,7 +127,8 @@ class MaxwellOperator:
         call("ef_theta", self._h, X.data_ptr(), Y.data_ptr(), m, ws.data_ptr(), ws.numel(),
              blas._stream())
         if tm is not None:
-            tm.end(ev, m, self.grid_size)
+            N = self.grid_size ** 3
+            tm.end("theta", ev, 32.0 * N * m + 4.0 * N, 630.0 * N * m, m)
         self.n_theta += m
         return Y
 
@@ -137,8 +138,13 @@ class MaxwellOperator:
         m = int(X.shape[0])
         Y = torch.empty_like(X) if out is None else out
         ws = self.workspace(m)
+        tm = profiling.active()
+        ev = tm.begin() if tm is not None else None
         call("ef_precondition", self._h, X.data_ptr(), Y.data_ptr(), m, ws.data_ptr(), ws.numel(),
              blas._stream())
+        if tm is not None:
+            N = self.grid_size ** 3
+            tm.end("precondition", ev, 32.0 * N * m + 4.0 * N, 630.0 * N * m, m)
         return Y
 
     def precondition_simple(self, Rs, target: float = 0.0) -> torch.Tensor:

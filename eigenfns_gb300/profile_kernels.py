@@ -1,0 +1,81 @@
+"""Small, self-contained kernel workloads for profiling (ncu) and quick timing.
+
+    python -m eigenfns_gb300.profile_kernels theta --grid 128 --m 2
+    python -m eigenfns_gb300.profile_kernels gram --ma 32 --mb 32 --grid 128
+    python -m eigenfns_gb300.profile_kernels rotate --ma 96 --mb 64 --grid 128
+    python -m eigenfns_gb300.profile_kernels cheb --grid 192 --m 8 --steps 8
+    python -m eigenfns_gb300.profile_kernels kpm --grid 256 --m 4 --steps 8
+
+Each runs 3 warm-up calls and then one timed call (CUDA events on the current
+stream), printing the time; under ncu, skip the warm-up launches with -s.
+Inputs are seeded random blocks and a seeded binary eps grid.
+"""
+from __future__ import annotations
+
+import argparse
+
+import numpy as np
+import torch
+
+
+def _op(G: int):
+    from .operator import MaxwellOperator
+    rng = np.random.default_rng(0)
+    eps = np.asarray(1.0 + 7.41 * (rng.random((G, G, G)) > 0.78), np.float32)
+    return MaxwellOperator(eps, 5.0)
+
+
+def _timed(fn, warm: int = 3) -> float:
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    fn()
+    e.record()
+    torch.cuda.synchronize()
+    return s.elapsed_time(e)
+
+
+def main(argv=None) -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("kernel", choices=["theta", "precond", "gram", "rotate", "cheb", "kpm"])
+    ap.add_argument("--grid", type=int, default=128)
+    ap.add_argument("--m", type=int, default=2)
+    ap.add_argument("--ma", type=int, default=32)
+    ap.add_argument("--mb", type=int, default=32)
+    ap.add_argument("--steps", type=int, default=4)
+    a = ap.parse_args(argv)
+    g = torch.Generator(device="cuda").manual_seed(1)
+    G = a.grid
+    if a.kernel in ("theta", "precond", "cheb", "kpm"):
+        op = _op(G)
+        X = torch.randn((a.m, 2, G, G, G), dtype=torch.complex64, device="cuda", generator=g)
+        Y = torch.empty_like(X)
+        if a.kernel == "theta":
+            ms = _timed(lambda: op.theta(X, out=Y))
+        elif a.kernel == "precond":
+            ms = _timed(lambda: op.precondition(X, out=Y))
+        elif a.kernel == "cheb":
+            from .interior import _apply_cheb_poly
+            coef = np.linspace(1.0, 0.1, a.steps + 1)
+            ms = _timed(lambda: _apply_cheb_poly(op, X, coef, 4.0e4))
+        else:
+            from .kpm import kpm_moments
+            ms = _timed(lambda: kpm_moments(op, 4.0e4, 2 * a.steps, a.m, Z=X))
+        print(f"{a.kernel} grid {G} m {a.m}: {ms:.3f} ms")
+    else:
+        from . import blas
+        K = 2 * G ** 3
+        A = torch.randn((a.ma, K), dtype=torch.complex64, device="cuda", generator=g)
+        B = torch.randn((a.mb, K), dtype=torch.complex64, device="cuda", generator=g)
+        if a.kernel == "gram":
+            ms = _timed(lambda: blas.gram(A, B))
+        else:
+            C = np.random.default_rng(2).standard_normal((a.ma, a.mb)).astype(np.complex64)
+            ms = _timed(lambda: blas.rotate(C, A, B))
+        print(f"{a.kernel} {a.ma}x{a.mb} K={K}: {ms:.3f} ms")
+
+
+if __name__ == "__main__":
+    main()

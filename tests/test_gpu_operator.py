@@ -238,3 +238,33 @@ def test_gram_shapes_match_numpy(gpu, ma, mb, K):
     got = blas.gram(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()).cpu().numpy()
     ref = A.astype(np.complex128).conj() @ B.astype(np.complex128).T
     assert np.abs(got - ref).max() < 2e-6 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("m_in,m_out,K,mode", [(96, 64, 2 * 32 ** 3, 0), (200, 32, 2 * 24 ** 3, 0),
+                                                (7, 5, 1002, 1), (33, 100, 2 * 16 ** 3 + 2, -1),
+                                                (40, 12, 2 * 16 ** 3 + 1, 0), (17, 20, 130, 1)])
+def test_rotate_shapes_and_modes_match_numpy(gpu, m_in, m_out, K, mode):
+    """Tiled (even K) and general (odd K) paths; row and column tails; set/add/subtract."""
+    from eigenfns_gb300 import blas
+    rng = np.random.default_rng(m_in * 7 + m_out)
+    S = (rng.standard_normal((m_in, K)) + 1j * rng.standard_normal((m_in, K))).astype(np.complex64)
+    C = (rng.standard_normal((m_in, m_out)) + 1j * rng.standard_normal((m_in, m_out))).astype(np.complex64)
+    O0 = (rng.standard_normal((m_out, K)) + 1j * rng.standard_normal((m_out, K))).astype(np.complex64)
+    ref = C.T.astype(np.complex128) @ S.astype(np.complex128)
+    if mode:
+        ref = O0 + mode * ref
+    out = torch.from_numpy(O0).cuda()
+    blas.rotate(C, torch.from_numpy(S).cuda(), out, mode)
+    assert np.abs(out.cpu().numpy() - ref).max() < 2e-6 * np.abs(ref).max() * np.sqrt(m_in)
+
+
+def test_rotate_in_place_m_out_32_tiled(gpu):
+    from eigenfns_gb300 import blas
+    rng = np.random.default_rng(3)
+    K = 2 * 32 ** 3
+    S = (rng.standard_normal((48, K)) + 1j * rng.standard_normal((48, K))).astype(np.complex64)
+    C = (rng.standard_normal((48, 32)) + 1j * rng.standard_normal((48, 32))).astype(np.complex64)
+    ref = C.T.astype(np.complex128) @ S.astype(np.complex128)
+    X = torch.from_numpy(S).cuda()
+    blas.rotate(C, X, X[:32])
+    assert np.abs(X[:32].cpu().numpy() - ref).max() < 2e-6 * np.abs(ref).max() * np.sqrt(48)

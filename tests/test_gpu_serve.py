@@ -1,0 +1,45 @@
+"""The request server: concurrent solves give the same results as solving alone.
+
+Each solve runs the same deterministic kernels on its own stream, so the
+eigenvalues served in a mix must equal those of the plain one-at-a-time path
+(compared at 1e-12 relative, i.e. bit-for-bit up to host LAPACK threading).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def _requests():
+    from eigenfns_gb300.serve import SolveRequest
+    return [SolveRequest(0, 64, 32, 11, 8, (0.1, -0.2, 0.3)),
+            SolveRequest(1, 64, 32, 12, 12, (0.0, 0.0, 0.0)),
+            SolveRequest(2, 216, 48, 13, 10, (0.25, 0.1, -0.4)),
+            SolveRequest(3, 64, 32, 14, 16, (-0.3, 0.45, 0.05), arrival=0.05)]
+
+
+def test_served_results_equal_solving_alone():
+    from eigenfns_gb300.serve import EigenServer, run_plain
+    reqs = _requests()
+    alone = run_plain(reqs)
+    srv = EigenServer(budget_bytes=40e9, max_concurrent=4)
+    served = srv.run(reqs, realtime=True)
+    assert srv.peak_concurrent >= 2
+    for a, b in zip(alone, served):
+        assert a.rid == b.rid and len(a.vals) == len(b.vals)
+        assert np.abs(a.vals - b.vals).max() <= 1e-12 * np.abs(a.vals).max()
+        assert b.max_res < 1e-4
+
+
+def test_admission_respects_the_budget():
+    from eigenfns_gb300.serve import EigenServer, footprint_bytes
+    reqs = _requests()[:3]
+    one = max(footprint_bytes(r) for r in reqs)
+    srv = EigenServer(budget_bytes=one * 1.01, max_concurrent=8)
+    res = srv.run(reqs, realtime=False)
+    assert srv.peak_concurrent == 1 and len(res) == 3
+    with pytest.raises(ValueError):
+        EigenServer(budget_bytes=one / 4).run(reqs, realtime=False)
