@@ -121,6 +121,14 @@ def rotate(C, S: torch.Tensor, out: torch.Tensor | None = None, mode: int = 0) -
     return out
 
 
+def tc_error() -> int:
+    """Reads and clears the tensor-core kernels' device error flag (synchronises)."""
+    import ctypes
+    flag = ctypes.c_int(0)
+    call("ef_tc_error", ctypes.addressof(flag))
+    return int(flag.value)
+
+
 def combine(C, *blocks: torch.Tensor) -> torch.Tensor:
     Cd = _coef(C, blocks[0].device)
     out = None

@@ -11,6 +11,7 @@
 // is flushed into an fp64 accumulator, and the chunks are reduced in fp64 in a
 // fixed order, so results are deterministic and the long sums keep fp64 accuracy.
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -689,6 +690,12 @@ int noalloc_scratch(void** out) {
 }
 }  // namespace
 
+namespace ef {
+int tc_rotate_max_rows(int m_out);
+int tc_rotate_launch(const float* C, int ldc, const float* S, float* out, int m_in, int m_out,
+                     long long K, int mode, cudaStream_t st);
+}  // namespace ef
+
 extern "C" {
 
 size_t ef_gram_workspace_bytes(int ma, int mb, long long K) {
@@ -754,7 +761,6 @@ int ef_gram_noalloc(const float* A, const float* B, int ma, int mb, long long K,
 int ef_rotate(const float* C, const float* S, float* out, int m_in, int m_out, long long K, int mode,
               void* stream) {
   if (!C || !S || !out || m_in <= 0 || m_out <= 0 || K <= 0) return ef_fail(EF_ERR_INVALID, "bad rotate arguments");
-  if ((size_t)m_in * RT * sizeof(float2) > 200 * 1024) return ef_fail(EF_ERR_TOO_LARGE, "m_in too large for rotate");
   const bool tiled = (K % 2 == 0) && ((((uintptr_t)S) | ((uintptr_t)out)) % 16 == 0);
   const int TIc = m_out <= 16 ? 2 : (m_out <= 32 ? 4 : 8);
   int ty = tiled ? (m_out + 8 * TIc - 1) / (8 * TIc) : (m_out + RT - 1) / RT;
@@ -766,6 +772,29 @@ int ef_rotate(const float* C, const float* S, float* out, int m_in, int m_out, l
   if (overlap && !(o0 == s0 && m_out <= 32 && ty == 1))
     return ef_fail(EF_ERR_INVALID, "rotate: out may alias S only exactly and with m_out <= 32");
   cudaStream_t st = (cudaStream_t)stream;
+  const char* kern = getenv("EF_ROTATE_KERNEL");
+  const bool simt = kern && strcmp(kern, "simt") == 0;
+  if (!simt) {
+    // tensor cores: output groups of <= 64 columns, row chunks of what one pass holds
+    if (overlap) {
+      if (m_in <= ef::tc_rotate_max_rows(m_out))
+        return ef::tc_rotate_launch(C, m_out, S, out, m_in, m_out, K, mode, st);
+    } else {
+      int rc = EF_OK;
+      for (int i0 = 0; i0 < m_out && rc == EF_OK; i0 += 64) {
+        const int mo = m_out - i0 < 64 ? m_out - i0 : 64;
+        const int rows = ef::tc_rotate_max_rows(mo);
+        for (int j0 = 0; j0 < m_in && rc == EF_OK; j0 += rows) {
+          const int mi = m_in - j0 < rows ? m_in - j0 : rows;
+          const int md = j0 == 0 ? mode : (mode == 0 ? 1 : mode);
+          rc = ef::tc_rotate_launch(C + 2 * ((long long)j0 * m_out + i0), m_out, S + 2 * (long long)j0 * K,
+                                    out + 2 * (long long)i0 * K, mi, mo, K, md, st);
+        }
+      }
+      return rc;
+    }
+  }
+  if ((size_t)m_in * RT * sizeof(float2) > 200 * 1024) return ef_fail(EF_ERR_TOO_LARGE, "m_in too large for rotate");
   if (tiled) {
     dim3 g((unsigned)((K + RK_KT - 1) / RK_KT), ty);
     ef_count_launches(1);

@@ -28,18 +28,16 @@
 
 #include "common.cuh"
 #include "status.h"
+#include "tc_common.cuh"
 
 namespace {
+
+using namespace ef::tc;
 
 constexpr int TC_THREADS = 128;
 constexpr int TC_KB = 32;            // real k-values (tf32) per stage = 16 complex
 constexpr int TC_M = 128;
 constexpr int TC_SEG = 8;            // stages per TMEM accumulation segment
-constexpr unsigned long long TC_SPIN_LIMIT = 1ull << 26;
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
 
 // byte offset of (row r, k-quad q) in an operand tile: core matrices of 8 rows x 16 B,
 // K-adjacent core matrices 128 B apart, 8-row groups (TC_KB/4)*128 = 1024 B apart
@@ -47,60 +45,8 @@ __device__ __forceinline__ int quad_off(int r, int q) {
   return (((r >> 3) * (TC_KB / 4) + q) << 7) + ((r & 7) << 4);
 }
 
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
-  const uint64_t lbo = 128, sbo = (TC_KB / 4) * 128;
-  uint64_t d = 0;
-  d |= (uint64_t)((addr >> 4) & 0x3FFF);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
-  d |= (uint64_t)1 << 46;               // descriptor version for tcgen05
-  return d;                             // base offset 0, no swizzle
-}
-
-// kind::tf32 instruction descriptor: D f32, A/B tf32, both K-major
-__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
-  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ float tf32_rn(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, int count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t a = smem_u32(bar);
-  for (unsigned long long it = 0; it < TC_SPIN_LIMIT; ++it) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (ok) return true;
-  }
-  return false;
-}
-
-__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,
-                                         uint32_t idesc, uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
-      ::"r"(dtmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-      : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-               ::"r"(smem_u32(bar)) : "memory");
+__device__ __forceinline__ uint64_t gram_desc(uint32_t addr) {
+  return smem_desc(addr, 128, (TC_KB / 4) * 128);
 }
 
 __host__ __device__ constexpr int tmem_cols(int nb) {
@@ -249,9 +195,9 @@ __global__ void __launch_bounds__(TC_THREADS) tc_gram_kernel(const float* __rest
 #pragma unroll
       for (int s = 0; s < TC_KB / 8; ++s) {   // 8 tf32 = 2 core matrices per MMA
         const uint32_t off = s * 256;
-        mma_tf32(d, smem_desc(aHi + off), smem_desc(bHi + off), idesc, (seg_first && s == 0) ? 0u : 1u);
-        mma_tf32(d, smem_desc(aHi + off), smem_desc(bLo + off), idesc, 1u);
-        mma_tf32(d, smem_desc(aLo + off), smem_desc(bHi + off), idesc, 1u);
+        mma_tf32(d, gram_desc(aHi + off), gram_desc(bHi + off), idesc, (seg_first && s == 0) ? 0u : 1u);
+        mma_tf32(d, gram_desc(aHi + off), gram_desc(bLo + off), idesc, 1u);
+        mma_tf32(d, gram_desc(aLo + off), gram_desc(bHi + off), idesc, 1u);
       }
       mma_commit(&stage_bar[buf]);
       if (seg_last) mma_commit(&seg_bar[seg & 1]);

@@ -100,6 +100,7 @@ class EigenServer:
         self._used = 0.0
         self._running = 0
         self.peak_concurrent = 0
+        self.peak_used = 0.0
         self.errors: list = []
 
     def _worker(self, req: SolveRequest, fp: float, t0: float, results: list, done: threading.Event):
@@ -145,6 +146,7 @@ class EigenServer:
                     self._used += fp
                     self._running += 1
                     self.peak_concurrent = max(self.peak_concurrent, self._running)
+                    self.peak_used = max(self.peak_used, self._used)
                     admitted = True
             if admitted:
                 th = threading.Thread(target=self._worker, args=(head, fp, t0, results, wake),

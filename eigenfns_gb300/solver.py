@@ -266,6 +266,8 @@ def lobpcg_blocks(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
         del Xl
     del slabs, HS
     torch.cuda.synchronize(dev)
+    if blas.tc_error():
+        raise RuntimeError("a tensor-core kernel timed out waiting on its pipeline; results invalid")
     stats.wall_seconds = time.perf_counter() - t0
     if locked_vals.size > 1 and (np.diff(locked_vals) < -1e-6 * np.abs(locked_vals[1:])).any():
         warnings.warn("locked eigenvalues non-monotone: a band was recovered out of order; "

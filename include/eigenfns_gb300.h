@@ -137,13 +137,19 @@ int ef_gram_noalloc(const float* A, const float* B, int ma, int mb, long long K,
 /* the same Gram on the tcgen05 tensor cores: 3xTF32 split products (fp32-class accuracy),
  * fp32 accumulation in TMEM per K-chunk, fp64 reduction across chunks. mb <= 256, K even,
  * 16-byte aligned rows. err_dev (device int) is set to 1 if a bounded wait timed out. */
+/* reads and clears the sticky device flag the tensor-core rotation sets when one of its
+ * bounded waits ran out (never expected; results of that call are not valid).
+ * Synchronises the device. */
+int ef_tc_error(int* flag);
 size_t ef_gram_tc_workspace_bytes(int ma, int mb, long long K);
 int ef_gram_tc(const float* A, const float* B, int ma, int mb, long long K, double* G, int* err_dev,
                void* work, size_t work_bytes, void* stream);
 /* out_i (+/-)= sum_j C[j][i] S_j, C complex64 (m_in, m_out) row-major:
  * combine / tensordot(C.T, S) (solver.py:49-57,106,125); mode 0 set, 1 add, -1 subtract.
  * `out` may be `S` itself when m_out <= 32 (each column k is read in full before it is
- * written); otherwise it must not overlap S (EF_ERR_INVALID). */
+ * written); otherwise it must not overlap S (EF_ERR_INVALID). Runs on the tcgen05
+ * tensor cores (3xTF32 split products, fp32-class accuracy); setting the environment
+ * variable EF_ROTATE_KERNEL=simt selects the fp32 CUDA-core kernel instead. */
 int ef_rotate(const float* C, const float* S, float* out, int m_in, int m_out, long long K,
               int mode, void* stream);
 /* work bytes of ef_rowdot and ef_rowstats for these sizes */

@@ -268,3 +268,23 @@ def test_rotate_in_place_m_out_32_tiled(gpu):
     X = torch.from_numpy(S).cuda()
     blas.rotate(C, X, X[:32])
     assert np.abs(X[:32].cpu().numpy() - ref).max() < 2e-6 * np.abs(ref).max() * np.sqrt(48)
+
+
+@pytest.mark.parametrize("m_in,m_out", [(96, 64), (200, 32), (32, 32), (300, 100)])
+def test_rotate_tensor_core_matches_cuda_core(gpu, m_in, m_out, monkeypatch):
+    """The 3xTF32 tensor-core kernel agrees with the fp32 CUDA-core kernel to fp32 rounding."""
+    from eigenfns_gb300 import blas
+    K = 2 * 32 ** 3
+    g = torch.Generator(device="cuda").manual_seed(m_in + m_out)
+    S = torch.randn((m_in, K), dtype=torch.complex64, device="cuda", generator=g)
+    C = np.random.default_rng(m_in).standard_normal((m_in, m_out, 2)).astype(np.float32)
+    C = (C[..., 0] + 1j * C[..., 1]).astype(np.complex64)
+    tc = blas.rotate(C, S)
+    monkeypatch.setenv("EF_ROTATE_KERNEL", "simt")
+    simt = blas.rotate(C, S)
+    monkeypatch.delenv("EF_ROTATE_KERNEL")
+    ref = C.T.astype(np.complex128) @ S.cpu().numpy().astype(np.complex128)
+    scale = np.abs(ref).max()
+    assert np.abs(tc.cpu().numpy() - ref).max() < 3e-6 * scale
+    assert np.abs(simt.cpu().numpy() - ref).max() < 3e-6 * scale
+    assert blas.tc_error() == 0

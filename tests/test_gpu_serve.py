@@ -37,9 +37,16 @@ def test_served_results_equal_solving_alone():
 def test_admission_respects_the_budget():
     from eigenfns_gb300.serve import EigenServer, footprint_bytes
     reqs = _requests()[:3]
-    one = max(footprint_bytes(r) for r in reqs)
-    srv = EigenServer(budget_bytes=one * 1.01, max_concurrent=8)
+    fps = [footprint_bytes(r) for r in reqs]
+    budget = max(fps) * 1.01
+    srv = EigenServer(budget_bytes=budget, max_concurrent=8)
     res = srv.run(reqs, realtime=False)
-    assert srv.peak_concurrent == 1 and len(res) == 3
+    assert len(res) == 3 and srv.peak_used <= budget
+    # two requests whose footprints do not fit together run one at a time
+    pair = _requests()[:2]
+    tight = max(footprint_bytes(r) for r in pair) * 1.01
+    assert tight < sum(footprint_bytes(r) for r in pair)
+    srv = EigenServer(budget_bytes=tight, max_concurrent=8)
+    assert len(srv.run(pair, realtime=False)) == 2 and srv.peak_concurrent == 1
     with pytest.raises(ValueError):
-        EigenServer(budget_bytes=one / 4).run(reqs, realtime=False)
+        EigenServer(budget_bytes=max(fps) / 4).run(reqs, realtime=False)
