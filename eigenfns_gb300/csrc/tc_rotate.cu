@@ -38,10 +38,13 @@ constexpr int TR_CONV = 256;              // converter threads (warps 0-7)
 constexpr int TR_EPI0 = 256;              // first epilogue thread (warps 8-11)
 constexpr int TR_MMA_WARP = 12;
 constexpr int TR_M = 128;                 // real positions per tile
-constexpr int TR_JC = 32;                 // rows of S per stage
+constexpr int TR_JC = 16;                 // rows of S per stage
 constexpr int TR_NBUF = 3;                // operand stages in the ring
-constexpr int TR_OP_HALF = TR_M * TR_JC * 4;       // 16 KB: hi or lo of one stage
-constexpr int TR_OP_BYTES = 2 * TR_OP_HALF;        // 32 KB per stage
+constexpr int TR_OP_HALF = TR_M * TR_JC * 4;       // 8 KB: hi or lo of one stage
+constexpr int TR_OP_BYTES = 2 * TR_OP_HALF;        // 16 KB per stage
+constexpr int TR_RAW = 8;                 // raw stages in flight per converter thread
+constexpr int TR_ROWS_T = TR_JC / 2;      // rows per converter thread per stage
+constexpr int TR_RAW_BYTES = TR_CONV * TR_ROWS_T * 4;   // 8 KB per raw stage
 constexpr int TR_SMEM_MAX = 227 * 1024 - 1024;   // dynamic part; static barriers take the rest
 
 __device__ int g_tc_error = 0;
@@ -55,7 +58,7 @@ struct TrArgs {
   int ldc, m_in, m_out, mp, nch, mode;
 };
 
-__global__ void __launch_bounds__(TR_THREADS, 1) tc_rotate_kernel(const TrArgs a) {
+__global__ void __maxnreg__(152) tc_rotate_kernel(const TrArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t op_full[TR_NBUF], op_empty[TR_NBUF];
   __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done_bar;
@@ -66,7 +69,8 @@ __global__ void __launch_bounds__(TR_THREADS, 1) tc_rotate_kernel(const TrArgs a
   const int N = 2 * a.mp;
   const int kj = a.nch * TR_JC;            // padded rows of the coefficient operand
   const uint32_t b_half = (uint32_t)N * kj * 4;
-  unsigned char* bops = smem + TR_NBUF * TR_OP_BYTES;
+  unsigned char* raw = smem + TR_NBUF * TR_OP_BYTES;
+  unsigned char* bops = raw + TR_RAW * TR_RAW_BYTES;
   const uint32_t tcols = tmem_cols_for(2 * N);
 
   if (tid == 0) {
@@ -113,28 +117,50 @@ __global__ void __launch_bounds__(TR_THREADS, 1) tc_rotate_kernel(const TrArgs a
 
   if (warp < 8) {
     // ---------------- converters ----------------
+    // Each thread owns one position p and TR_ROWS_T rows of every stage. Its values
+    // travel through a private ring of TR_RAW raw stages (4-byte cp.async, zero-fill
+    // outside the matrix), so TR_RAW stages of loads are in flight without holding
+    // registers; the thread then splits hi/lo and stores 16-byte quads.
     const int p = tid & (TR_M - 1), h = tid >> 7;
-    auto load = [&](long long s, float (&v)[16]) {
-      if (s >= nstages) return;
-      const long long tile = blockIdx.x + (s / a.nch) * (long long)gridDim.x;
-      const int c = (int)(s % a.nch);
-      const long long pos = tile * TR_M + p;
-      const int j0 = c * TR_JC + h * 16;
-      const bool pin = pos < a.n2;
+    auto issue = [&](long long s) {
+      if (s < nstages) {
+        const long long tile = blockIdx.x + (s / a.nch) * (long long)gridDim.x;
+        const int c = (int)(s % a.nch);
+        const long long pos = tile * TR_M + p;
+        const int j0 = c * TR_JC + h * TR_ROWS_T;
+        const bool pin = pos < a.n2;
+        const uint32_t slot = smem_u32(raw + (int)(s % TR_RAW) * TR_RAW_BYTES) + tid * 4;
 #pragma unroll
-      for (int r = 0; r < 16; ++r) {
-        const int j = j0 + r;
-        v[r] = (pin && j < a.m_in) ? a.S[(long long)j * a.n2 + pos] : 0.f;
+        for (int r = 0; r < TR_ROWS_T; ++r) {
+          const int j = j0 + r;
+          const bool in = pin && j < a.m_in;
+          const float* g = a.S + (in ? (long long)j * a.n2 + pos : 0);
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(slot + r * TR_CONV * 4),
+                       "l"(g), "r"(in ? 4 : 0) : "memory");
+        }
       }
+      asm volatile("cp.async.commit_group;" ::: "memory");
     };
-    auto store = [&](long long s, const float (&v)[16]) -> bool {
+    for (long long s = 0; s < TR_RAW - 1; ++s) issue(s);
+    for (long long s = 0; s < nstages; ++s) {
+      if (abort_s) break;
+      issue(s + TR_RAW - 1);
+      asm volatile("cp.async.wait_group %0;" ::"n"(TR_RAW - 1) : "memory");
+      const float* rs = reinterpret_cast<const float*>(raw + (int)(s % TR_RAW) * TR_RAW_BYTES) + tid;
+      float v[TR_ROWS_T];
+#pragma unroll
+      for (int r = 0; r < TR_ROWS_T; ++r) v[r] = rs[r * TR_CONV];
       const int o = (int)(s % TR_NBUF);
       const uint32_t u = (uint32_t)(s / TR_NBUF);
-      if (!mbar_wait(&op_empty[o], (u + 1) & 1)) return false;
+      if (!mbar_wait(&op_empty[o], (u + 1) & 1)) {
+        abort_s = 1;
+        atomicExch(&g_tc_error, 1);
+        break;
+      }
       unsigned char* base = smem + o * TR_OP_BYTES;
 #pragma unroll
-      for (int qq = 0; qq < 4; ++qq) {
-        const int q = h * 4 + qq;
+      for (int qq = 0; qq < TR_ROWS_T / 4; ++qq) {
+        const int q = h * (TR_ROWS_T / 4) + qq;
         const float4 x = make_float4(v[4 * qq], v[4 * qq + 1], v[4 * qq + 2], v[4 * qq + 3]);
         const float4 hi = make_float4(tf32_rn(x.x), tf32_rn(x.y), tf32_rn(x.z), tf32_rn(x.w));
         const float4 lo = make_float4(tf32_rn(x.x - hi.x), tf32_rn(x.y - hi.y), tf32_rn(x.z - hi.z),
@@ -145,41 +171,33 @@ __global__ void __launch_bounds__(TR_THREADS, 1) tc_rotate_kernel(const TrArgs a
       }
       fence_async_smem();
       mbar_arrive(&op_full[o]);
-      return true;
-    };
-    float v0[16], v1[16], v2[16];
-    load(0, v0);
-    load(1, v1);
-    for (long long s = 0; s < nstages; s += 3) {
-      if (abort_s) break;
-      load(s + 2, v2);
-      if (!store(s, v0)) { abort_s = 1; atomicExch(&g_tc_error, 1); break; }
-      if (s + 1 >= nstages) break;
-      load(s + 3, v0);
-      if (!store(s + 1, v1)) { abort_s = 1; atomicExch(&g_tc_error, 1); break; }
-      if (s + 2 >= nstages) break;
-      load(s + 4, v1);
-      if (!store(s + 2, v2)) { abort_s = 1; atomicExch(&g_tc_error, 1); break; }
     }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
   } else if (warp < 12) {
     // ---------------- epilogue ----------------
+    // For the accumulate modes the current output values of the first 32 rows are
+    // loaded before the wait for the accumulator, so their latency overlaps the MMAs.
     const int p = tid - TR_EPI0;                       // = 32 * (warp % 4) + lane
     const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
     const bool even = (p & 1) == 0;
     for (long long k = 0; k < my_tiles; ++k) {
       if (abort_s) break;
       const int ab = (int)(k & 1);
+      const long long tile = blockIdx.x + k * (long long)gridDim.x;
+      const long long pos = tile * TR_M + p;
+      const bool pin = pos < a.n2;
+      float prev[32];
+#pragma unroll
+      for (int t = 0; t < 32; ++t)
+        prev[t] = (a.mode != 0 && pin && t < a.m_out) ? a.out[(long long)t * a.n2 + pos] : 0.f;
       if (!mbar_wait(&acc_full[ab], (uint32_t)((k >> 1) & 1))) {
         abort_s = 1;
         atomicExch(&g_tc_error, 1);
         break;
       }
       fence_after_sync();
-      const long long tile = blockIdx.x + k * (long long)gridDim.x;
-      const long long pos = tile * TR_M + p;
-      const bool pin = pos < a.n2;
       const uint32_t ta = lane_base + (uint32_t)(ab * N);
-      for (int i0 = 0; i0 < a.mp; i0 += 8) {
+      auto emit = [&](int i0, const float (&pv)[8]) {
         float d1[8], d2[8];
         tmem_ld8x2(ta + i0, ta + a.mp + i0, d1, d2);
 #pragma unroll
@@ -190,10 +208,26 @@ __global__ void __launch_bounds__(TR_THREADS, 1) tc_rotate_kernel(const TrArgs a
           if (pin && i < a.m_out) {
             float* o = a.out + (long long)i * a.n2 + pos;
             if (a.mode == 0) *o = val;
-            else if (a.mode > 0) *o = *o + val;
-            else *o = *o - val;
+            else if (a.mode > 0) *o = pv[t] + val;
+            else *o = pv[t] - val;
           }
         }
+      };
+#pragma unroll
+      for (int c8 = 0; c8 < 4; ++c8) {          // rows 0..31: prefetched values
+        if (c8 * 8 < a.mp) {
+          float pv[8];
+#pragma unroll
+          for (int t = 0; t < 8; ++t) pv[t] = prev[c8 * 8 + t];
+          emit(c8 * 8, pv);
+        }
+      }
+      for (int i0 = 32; i0 < a.mp; i0 += 8) {  // rows 32..63
+        float pv[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t)
+          pv[t] = (a.mode != 0 && pin && i0 + t < a.m_out) ? a.out[(long long)(i0 + t) * a.n2 + pos] : 0.f;
+        emit(i0, pv);
       }
       fence_before_sync();
       mbar_arrive(&acc_empty[ab]);
@@ -268,7 +302,8 @@ int sm_count() {
 
 size_t tr_smem(int m_in, int mp) {
   const int nch = (m_in + TR_JC - 1) / TR_JC;
-  return (size_t)TR_NBUF * TR_OP_BYTES + (size_t)2 * (2 * mp) * (nch * TR_JC) * 4;
+  return (size_t)TR_NBUF * TR_OP_BYTES + (size_t)TR_RAW * TR_RAW_BYTES +
+         (size_t)2 * (2 * mp) * (nch * TR_JC) * 4;
 }
 
 }  // namespace
