@@ -4,23 +4,26 @@
 // products over the interleaved (re, im) storage:
 //   Re G = A_r . B_r^T            A_r[i] = (ar0, ai0, ar1, ai1, ...)
 //   Im G = A'_r . B_r^T           A'_r[i] = (-ai0, ar0, -ai1, ar1, ...)
-// Rows [0, 64) of the M = 128 MMA operand hold up to 64 rows of A, rows [64, 128)
-// the matching rows of A'; a CTA covers 64 rows of A and NB <= 64 rows of B
-// (larger shapes tile over grid.x / grid.y). Three TF32 products per pair give
-// fp32-class products (x = hi + lo, hi = round-to-tf32(x)):
-//   D += A_hi B_hi + A_hi B_lo + A_lo B_hi        (.kind::tf32, fp32 accumulate)
-// Tensor-core fp32 accumulation is not round-to-nearest over long chains, so a
-// CTA's K-chunk is cut into segments of SEG stages that accumulate alternately
-// into two TMEM regions; every finished segment is read back (tcgen05.ld) and
-// added into fp64 registers, one TMEM lane (= one row) per thread, while the
-// next segment's MMAs run in the other region. Chunks are reduced in fp64.
+// The M = 128 operand holds up to MT (32 or 64) rows of A in rows [0, MT) and the
+// matching rows of A' in [MT, 2MT); the N operand holds NB rows of B as
+// [B_hi; B_lo]. Per 8-real k-step two MMAs give fp32-class products (x = hi + lo):
+//   D[:, 0:2NB]  += A_hi [B_hi; B_lo]^T      (hh | hl)
+//   D[:, NB:2NB] += A_lo B_hi^T              (hl + lh)
+// Tensor-core fp32 accumulation is not round-to-nearest over long chains, so the
+// accumulation is cut into segments of SEG stages, alternating between two TMEM
+// accumulators; each finished segment is read back (tcgen05.ld) and added into fp32
+// registers while the next segment's MMAs run; a work unit's sum goes out in fp64
+// and units (K-chunks) are reduced in fp64.
 //
-// Pipeline per 16-complex stage: all 128 threads convert the stage they prefetched
-// into registers (hi/lo split, A' swap) and store it with 16-byte stores into the
-// no-swizzle K-major core-matrix layout, prefetch the next stage, fence the
-// async proxy, and thread 0 issues the stage's 12 MMAs and commits them to the
-// stage buffer's mbarrier. Every mbarrier wait is bounded; on timeout the kernel
-// sets an error flag, skips the rest, frees its TMEM and returns.
+// A persistent CTA (288 threads) walks work units (A-tile, B-tile, K-chunk):
+//   warps 0-3    converters: 16-byte cp.async of their (row, quad) items into a
+//                private 4-deep raw ring, hi/lo split (and the A' swap), 16-byte
+//                stores into a 3-deep ring of K-major operand stages;
+//   warp 8       one thread issues each stage's MMAs and commits them;
+//   warps 4-7    drain finished segments (one TMEM lane per thread, all columns)
+//                and write the unit's partial sums.
+// Every mbarrier wait is bounded; on timeout the kernel sets the error flag, stops,
+// waits (bounded) for its own MMAs and frees its TMEM.
 //
 // Reference: gram, eigenfns/solver.py:35-43 (true-fp32 X^H Y; the reference
 // forbids plain TF32, which floors the Gram at ~1e-3).
@@ -34,248 +37,386 @@ namespace {
 
 using namespace ef::tc;
 
-constexpr int TC_THREADS = 128;
-constexpr int TC_KB = 32;            // real k-values (tf32) per stage = 16 complex
-constexpr int TC_M = 128;
-constexpr int TC_SEG = 8;            // stages per TMEM accumulation segment
+constexpr int GC_THREADS = 288;
+constexpr int GC_CONV = 128;          // converter threads (warps 0-3)
+constexpr int GC_MMA_WARP = 8;
+constexpr int GC_KB = 32;             // reals per stage (16 complex) = 4 k-steps of 8
+constexpr int GC_NBUF = 3;            // operand stages
+constexpr int GC_RAW = 4;             // raw stages per converter thread
+constexpr int GC_SEG = 8;             // stages per TMEM accumulation segment
+constexpr int GC_A_HALF = 128 * GC_KB * 4;   // 16 KB: A_hi or A_lo of one stage
 
 // byte offset of (row r, k-quad q) in an operand tile: core matrices of 8 rows x 16 B,
-// K-adjacent core matrices 128 B apart, 8-row groups (TC_KB/4)*128 = 1024 B apart
+// K-adjacent core matrices 128 B apart, 8-row groups (GC_KB/4)*128 = 1024 B apart
 __device__ __forceinline__ int quad_off(int r, int q) {
-  return (((r >> 3) * (TC_KB / 4) + q) << 7) + ((r & 7) << 4);
+  return (((r >> 3) * (GC_KB / 4) + q) << 7) + ((r & 7) << 4);
 }
 
 __device__ __forceinline__ uint64_t gram_desc(uint32_t addr) {
-  return smem_desc(addr, 128, (TC_KB / 4) * 128);
+  return smem_desc(addr, 128, (GC_KB / 4) * 128);
 }
 
-__host__ __device__ constexpr int tmem_cols(int nb) {
-  return 2 * nb <= 32 ? 32 : (2 * nb <= 64 ? 64 : (2 * nb <= 128 ? 128 : 256));
-}
+struct GcArgs {
+  const float* A;
+  const float* B;
+  double* partial;      // entry-major (ma*mb, nk) double2
+  int* err;
+  long long K;          // complex values per row
+  long long kchunk;     // complex values per unit (multiple of 16)
+  int ma, mb, mt, nit, njt, nk;
+};
 
+// 9 warps: at most 3 per SM sub-partition, so 168 registers a thread still fit
 template <int NB>
-__global__ void __launch_bounds__(TC_THREADS) tc_gram_kernel(const float* __restrict__ A,
-                                                             const float* __restrict__ B, int ma,
-                                                             int mb, long long K, long long kchunk,
-                                                             double* __restrict__ partial,
-                                                             int* __restrict__ err) {
-  constexpr int TILE_A = TC_M * TC_KB * 4;      // 16 KB
-  constexpr int TILE_B = NB * TC_KB * 4;
-  constexpr int STAGE = 2 * TILE_A + 2 * TILE_B;
-  constexpr int ITEMS_MAX = (64 + NB) * 8;       // float4 per stage
-  constexpr int PER_T = (ITEMS_MAX + TC_THREADS - 1) / TC_THREADS;
+__global__ void __maxnreg__(168) tc_gram_kernel(const GcArgs a) {
+  constexpr int B_BYTES = 2 * NB * GC_KB * 4;                  // [B_hi; B_lo]
+  constexpr int OP_BYTES = 2 * GC_A_HALF + B_BYTES;
+  constexpr int IPT = ((64 + NB) * (GC_KB / 4) + GC_CONV - 1) / GC_CONV;   // items per thread
+  constexpr int RAW_BYTES = IPT * GC_CONV * 16;
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(8) uint64_t stage_bar[2];
-  __shared__ __align__(8) uint64_t seg_bar[2];
+  __shared__ __align__(8) uint64_t op_full[GC_NBUF], op_empty[GC_NBUF];
+  __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done_bar;
   __shared__ uint32_t tmem_base_s;
-  __shared__ int abort_s;
+  __shared__ volatile int abort_s;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int i0 = blockIdx.x * 64, j0 = blockIdx.y * NB;
-  const int mrows = (ma - i0) < 64 ? (ma - i0) : 64;
-  const int nrows = (mb - j0) < NB ? (mb - j0) : NB;
-  const long long kbeg = (long long)blockIdx.z * kchunk;
-  long long kend = kbeg + kchunk;
-  if (kend > K) kend = K;
-  const int nst = (int)((kend - kbeg + (TC_KB / 2) - 1) / (TC_KB / 2));
-  const int items = (mrows + nrows) * 8;
+  unsigned char* raw = smem + GC_NBUF * OP_BYTES;
+  constexpr uint32_t TCOLS = tmem_cols_for(4 * NB);
+  const int nitems = (a.mt + NB) * (GC_KB / 4);                // items per stage
+  const long long units = (long long)a.nit * a.njt * a.nk;
+  const long long my_units = units > blockIdx.x ? (units - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
 
   if (tid == 0) {
     abort_s = 0;
-    mbar_init(&stage_bar[0], 1);
-    mbar_init(&stage_bar[1], 1);
-    mbar_init(&seg_bar[0], 1);
-    mbar_init(&seg_bar[1], 1);
+    for (int b = 0; b < GC_NBUF; ++b) {
+      mbar_init(&op_full[b], GC_CONV);
+      mbar_init(&op_empty[b], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], 128);
+    }
+    mbar_init(&done_bar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  for (int e = tid; e < 2 * STAGE / 16; e += TC_THREADS)
+  // operand rows the converters never write (A rows >= 2*mt) must read as zero
+  for (int e = tid; e < GC_NBUF * OP_BYTES / 16; e += GC_THREADS)
     reinterpret_cast<float4*>(smem)[e] = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                 ::"r"(smem_u32(&tmem_base_s)), "r"(tmem_cols(NB)) : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  fence_async_smem();
+  if (warp == GC_MMA_WARP) tmem_alloc(&tmem_base_s, TCOLS);
+  fence_before_sync();
   __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  fence_after_sync();
   const uint32_t tmem = tmem_base_s;
-  const uint32_t idesc = idesc_tf32(TC_M, NB);
 
-  // stage loads: item e -> (row, quad q): rows [0, mrows) of A then [0, nrows) of B
-  float4 pre[PER_T];
-  auto prefetch = [&](int st) {
-    const long long kc0 = kbeg + (long long)st * (TC_KB / 2);
-#pragma unroll
-    for (int u = 0; u < PER_T; ++u) {
-      const int e = tid + u * TC_THREADS;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (e < items) {
-        const int r = e >> 3, q = e & 7;
-        const long long kc = kc0 + 2 * q;
-        const float* src = (r < mrows) ? A + ((long long)(i0 + r) * K + kc) * 2
-                                       : B + ((long long)(j0 + r - mrows) * K + kc) * 2;
-        if (kc + 1 < kend) v = __ldg(reinterpret_cast<const float4*>(src));
-        else if (kc < kend) v = make_float4(__ldg(src), __ldg(src + 1), 0.f, 0.f);
+  // k-th unit of this CTA -> (A-tile, B-tile, K-chunk), first complex index, stages
+  auto unit_of = [&](long long k, int& it, int& jt, int& kc, long long& kbeg, int& nst) {
+    const long long u = blockIdx.x + k * (long long)gridDim.x;
+    kc = (int)(u % a.nk);
+    const long long t = u / a.nk;
+    jt = (int)(t % a.njt);
+    it = (int)(t / a.njt);
+    kbeg = (long long)kc * a.kchunk;
+    long long kend = kbeg + a.kchunk;
+    if (kend > a.K) kend = a.K;
+    nst = kend > kbeg ? (int)((kend - kbeg + GC_KB / 2 - 1) / (GC_KB / 2)) : 0;
+  };
+
+  if (warp < 4) {
+    // ---------------- converters ----------------
+    // item e of a stage: row r = e % (mt + NB), quad q = e / (mt + NB); rows [0, mt) are
+    // A rows, [mt, mt + NB) B rows. Consecutive threads take consecutive rows, so the
+    // 16-byte operand stores of 8 threads fill one 128-byte core-matrix line.
+    const int rows = a.mt + NB;
+    long long s_issue = 0;
+    long long ku = 0;                                // issue cursor: unit, stage in unit
+    int it = 0, jt = 0, kc = 0, nst = 0, st_in = 0;
+    long long kbeg = 0;
+    if (my_units > 0) unit_of(0, it, jt, kc, kbeg, nst);
+    auto issue = [&]() {
+      while (ku < my_units && st_in >= nst) {
+        ++ku;
+        st_in = 0;
+        if (ku < my_units) unit_of(ku, it, jt, kc, kbeg, nst);
       }
-      pre[u] = v;
+      if (ku < my_units) {
+        const int i0 = it * a.mt, j0 = jt * NB;
+        const long long kc0 = kbeg + (long long)st_in * (GC_KB / 2);
+        long long kend = kbeg + a.kchunk;
+        if (kend > a.K) kend = a.K;
+        const uint32_t slot = smem_u32(raw + (int)(s_issue % GC_RAW) * RAW_BYTES) + tid * 16;
+#pragma unroll
+        for (int u = 0; u < IPT; ++u) {
+          const int e = tid + u * GC_CONV;
+          const int r = e % rows, q = e / rows;
+          const long long kq = kc0 + 2 * q;
+          bool in = e < nitems && kq < kend;
+          const float* g = a.A;
+          if (in) {
+            if (r < a.mt) {
+              in = i0 + r < a.ma;
+              g = a.A + ((long long)(i0 + r) * a.K + kq) * 2;
+            } else {
+              in = j0 + r - a.mt < a.mb;
+              g = a.B + ((long long)(j0 + r - a.mt) * a.K + kq) * 2;
+            }
+          }
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(slot + u * GC_CONV * 16),
+                       "l"(in ? g : a.A), "r"(in ? 16 : 0) : "memory");
+        }
+        ++st_in;
+        ++s_issue;
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    long long total = 0;
+    for (long long k = 0; k < my_units; ++k) {
+      int i1, j1, k1, n1;
+      long long b1;
+      unit_of(k, i1, j1, k1, b1, n1);
+      total += n1;
     }
-  };
-  double acc[NB];
-#pragma unroll
-  for (int c = 0; c < NB; ++c) acc[c] = 0.0;
-  uint32_t sph[2] = {0u, 0u}, gph[2] = {0u, 0u};
-  int drained = 0;   // segments already added into acc
-  const int nseg = (nst + TC_SEG - 1) / TC_SEG;
-
-  auto drain = [&](int seg) -> bool {
-    const int reg = seg & 1;
-    if (!mbar_wait(&seg_bar[reg], gph[reg])) return false;
-    gph[reg] ^= 1u;
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(reg * NB);
-#pragma unroll
-    for (int c0 = 0; c0 < NB; c0 += 8) {
-      uint32_t v[8];
-      asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                   : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
-                     "=r"(v[6]), "=r"(v[7])
-                   : "r"(taddr + c0));
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-      for (int t = 0; t < 8; ++t) acc[c0 + t] += (double)__uint_as_float(v[t]);
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    return true;
-  };
-
-  if (nst > 0) prefetch(0);
-  for (int st = 0; st < nst; ++st) {
-    const int buf = st & 1;
-    unsigned char* sb = smem + buf * STAGE;
-    if (st >= 2) {
-      if (tid == 0 && !mbar_wait(&stage_bar[buf], sph[buf])) abort_s = 1;
-      sph[buf] ^= 1u;
-      __syncthreads();
+    for (int s = 0; s < GC_RAW - 1; ++s) issue();
+    for (long long s = 0; s < total; ++s) {
       if (abort_s) break;
-    }
-    // convert the prefetched stage: A rows -> (A, A') hi/lo, B rows -> B hi/lo
+      issue();
+      asm volatile("cp.async.wait_group %0;" ::"n"(GC_RAW - 1) : "memory");
+      const float4* rs = reinterpret_cast<const float4*>(raw + (int)(s % GC_RAW) * RAW_BYTES) + tid;
+      float4 v[IPT];
 #pragma unroll
-    for (int u = 0; u < PER_T; ++u) {
-      const int e = tid + u * TC_THREADS;
-      if (e < items) {
-        const int r = e >> 3, q = e & 7;
-        const float4 v = pre[u];
-        const float4 h = make_float4(tf32_rn(v.x), tf32_rn(v.y), tf32_rn(v.z), tf32_rn(v.w));
-        const float4 l = make_float4(tf32_rn(v.x - h.x), tf32_rn(v.y - h.y), tf32_rn(v.z - h.z),
-                                     tf32_rn(v.w - h.w));
-        if (r < mrows) {
-          *reinterpret_cast<float4*>(sb + quad_off(r, q)) = h;
-          *reinterpret_cast<float4*>(sb + TILE_A + quad_off(r, q)) = l;
-          // A' = (-ai, ar) per complex: swap within the pairs and negate the new real part
-          *reinterpret_cast<float4*>(sb + quad_off(64 + r, q)) = make_float4(-h.y, h.x, -h.w, h.z);
-          *reinterpret_cast<float4*>(sb + TILE_A + quad_off(64 + r, q)) = make_float4(-l.y, l.x, -l.w, l.z);
-        } else {
-          const int rb = r - mrows;
-          *reinterpret_cast<float4*>(sb + 2 * TILE_A + quad_off(rb, q)) = h;
-          *reinterpret_cast<float4*>(sb + 2 * TILE_A + TILE_B + quad_off(rb, q)) = l;
+      for (int u = 0; u < IPT; ++u) v[u] = rs[u * GC_CONV];
+      const int o = (int)(s % GC_NBUF);
+      if (!mbar_wait(&op_empty[o], (uint32_t)(((s / GC_NBUF) + 1) & 1))) {
+        abort_s = 1;
+        atomicExch(a.err, 1);
+        break;
+      }
+      unsigned char* base = smem + o * OP_BYTES;
+#pragma unroll
+      for (int u = 0; u < IPT; ++u) {
+        const int e = tid + u * GC_CONV;
+        if (e < nitems) {
+          const int r = e % rows, q = e / rows;
+          const float4 x = v[u];
+          const float4 h = make_float4(tf32_rn(x.x), tf32_rn(x.y), tf32_rn(x.z), tf32_rn(x.w));
+          const float4 l = make_float4(tf32_rn(x.x - h.x), tf32_rn(x.y - h.y), tf32_rn(x.z - h.z),
+                                       tf32_rn(x.w - h.w));
+          if (r < a.mt) {
+            *reinterpret_cast<float4*>(base + quad_off(r, q)) = h;
+            *reinterpret_cast<float4*>(base + GC_A_HALF + quad_off(r, q)) = l;
+            // A' = (-ai, ar) per complex: swap within the pairs and negate the new real part
+            *reinterpret_cast<float4*>(base + quad_off(a.mt + r, q)) = make_float4(-h.y, h.x, -h.w, h.z);
+            *reinterpret_cast<float4*>(base + GC_A_HALF + quad_off(a.mt + r, q)) =
+                make_float4(-l.y, l.x, -l.w, l.z);
+          } else {
+            const int rb = r - a.mt;
+            *reinterpret_cast<float4*>(base + 2 * GC_A_HALF + quad_off(rb, q)) = h;
+            *reinterpret_cast<float4*>(base + 2 * GC_A_HALF + quad_off(NB + rb, q)) = l;
+          }
+        }
+      }
+      fence_async_smem();
+      mbar_arrive(&op_full[o]);
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+  } else if (warp < 8) {
+    // ---------------- drain ----------------
+    const int lq = warp & 3;
+    const int L = lq * 32 + lane;                       // TMEM lane = M row
+    const uint32_t lane_base = tmem + ((uint32_t)(lq * 32) << 16);
+    float acc[NB];
+#pragma unroll
+    for (int c = 0; c < NB; ++c) acc[c] = 0.f;
+    long long q = 0;                                    // segment counter
+    for (long long k = 0; k < my_units && !abort_s; ++k) {
+      int it, jt, kc, nst;
+      long long kbeg;
+      unit_of(k, it, jt, kc, kbeg, nst);
+      const int nseg = (nst + GC_SEG - 1) / GC_SEG;
+      for (int sg = 0; sg < nseg; ++sg, ++q) {
+        const int ab = (int)(q & 1);
+        if (!mbar_wait(&acc_full[ab], (uint32_t)((q >> 1) & 1))) {
+          abort_s = 1;
+          atomicExch(a.err, 1);
+          break;
+        }
+        fence_after_sync();
+        const uint32_t ta = lane_base + (uint32_t)(ab * 2 * NB);
+#pragma unroll
+        for (int c0 = 0; c0 < NB; c0 += 8) {
+          float d1[8], d2[8];
+          tmem_ld8x2(ta + c0, ta + NB + c0, d1, d2);
+#pragma unroll
+          for (int t = 0; t < 8; ++t) acc[c0 + t] += d1[t] + d2[t];
+        }
+        fence_before_sync();
+        mbar_arrive(&acc_empty[ab]);
+      }
+      if (abort_s) break;
+      // unit partial: lanes [0, mt) Re of A rows, [mt, 2mt) Im
+      const bool re = L < a.mt, im = L >= a.mt && L < 2 * a.mt;
+      const int i = it * a.mt + (re ? L : L - a.mt);
+      if ((re || im) && i < a.ma) {
+#pragma unroll
+        for (int c = 0; c < NB; ++c) {
+          const int j = jt * NB + c;
+          if (j < a.mb)
+            a.partial[(((long long)i * a.mb + j) * a.nk + kc) * 2 + (re ? 0 : 1)] = (double)acc[c];
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < NB; ++c) acc[c] = 0.f;
+    }
+  } else if (warp == GC_MMA_WARP && lane == 0) {
+    // ---------------- MMA issue ----------------
+    const uint32_t id1 = idesc_tf32(128, 2 * NB), id2 = idesc_tf32(128, NB);
+    long long s = 0, q = 0;
+    bool issued = false;
+    for (long long k = 0; k < my_units && !abort_s; ++k) {
+      int it, jt, kc, nst;
+      long long kbeg;
+      unit_of(k, it, jt, kc, kbeg, nst);
+      for (int st = 0; st < nst; ++st, ++s) {
+        const bool seg_first = (st % GC_SEG) == 0;
+        const bool seg_last = (st % GC_SEG) == GC_SEG - 1 || st == nst - 1;
+        const int ab = (int)(q & 1);
+        if (seg_first && !mbar_wait(&acc_empty[ab], (uint32_t)(((q >> 1) + 1) & 1))) {
+          abort_s = 1;
+          atomicExch(a.err, 1);
+          break;
+        }
+        const int o = (int)(s % GC_NBUF);
+        if (!mbar_wait(&op_full[o], (uint32_t)((s / GC_NBUF) & 1))) {
+          abort_s = 1;
+          atomicExch(a.err, 1);
+          break;
+        }
+        fence_after_sync();
+        const uint32_t d = tmem + (uint32_t)(ab * 2 * NB);
+        const uint32_t aHi = smem_u32(smem + o * OP_BYTES), aLo = aHi + GC_A_HALF;
+        const uint32_t bB = aHi + 2 * GC_A_HALF;
+#pragma unroll
+        for (int g = 0; g < GC_KB / 8; ++g) {
+          const uint32_t off = g * 256;
+          mma_tf32(d, gram_desc(aHi + off), gram_desc(bB + off), id1, (seg_first && g == 0) ? 0u : 1u);
+          mma_tf32(d + NB, gram_desc(aLo + off), gram_desc(bB + off), id2, 1u);
+        }
+        mma_commit(&op_empty[o]);
+        issued = true;
+        if (seg_last) {
+          mma_commit(&acc_full[ab]);
+          ++q;
         }
       }
     }
-    if (st + 1 < nst) prefetch(st + 1);
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    const int seg = st / TC_SEG;
-    const bool seg_first = (st % TC_SEG) == 0;
-    const bool seg_last = ((st % TC_SEG) == TC_SEG - 1) || (st == nst - 1);
-    if (tid == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t d = tmem + (uint32_t)((seg & 1) * NB);
-      const uint32_t aHi = smem_u32(sb), aLo = smem_u32(sb + TILE_A);
-      const uint32_t bHi = smem_u32(sb + 2 * TILE_A), bLo = smem_u32(sb + 2 * TILE_A + TILE_B);
-#pragma unroll
-      for (int s = 0; s < TC_KB / 8; ++s) {   // 8 tf32 = 2 core matrices per MMA
-        const uint32_t off = s * 256;
-        mma_tf32(d, gram_desc(aHi + off), gram_desc(bHi + off), idesc, (seg_first && s == 0) ? 0u : 1u);
-        mma_tf32(d, gram_desc(aHi + off), gram_desc(bLo + off), idesc, 1u);
-        mma_tf32(d, gram_desc(aLo + off), gram_desc(bHi + off), idesc, 1u);
-      }
-      mma_commit(&stage_bar[buf]);
-      if (seg_last) mma_commit(&seg_bar[seg & 1]);
-    }
-    // one stage into a segment, drain the previous one (its region is reused two segments on)
-    if ((st % TC_SEG) == 1 && seg >= 1 && drained == seg - 1) {
-      if (!drain(seg - 1)) atomicExch(&abort_s, 1);
-      ++drained;
+    if (abort_s && issued) {
+      mma_commit(&done_bar);
+      mbar_wait(&done_bar, 0);
     }
   }
+  fence_before_sync();
   __syncthreads();
-  if (!abort_s) {
-    while (drained < nseg) {
-      if (!drain(drained)) { abort_s = 1; break; }
-      ++drained;
-    }
-  }
-  __syncthreads();
-  if (!abort_s && nst > 0) {
-    const int row = warp * 32 + lane;
-    double* out = partial + (long long)blockIdx.z * ma * mb * 2;
-    const bool re = row < mrows, im = row >= 64 && row - 64 < mrows;
-    const int i = i0 + (re ? row : row - 64);
-#pragma unroll
-    for (int c = 0; c < NB; ++c) {
-      if (c < nrows) {
-        if (re) out[((long long)i * mb + j0 + c) * 2] = acc[c];
-        if (im) out[((long long)i * mb + j0 + c) * 2 + 1] = acc[c];
-      }
-    }
-  } else if (abort_s && tid == 0) {
-    atomicExch(err, 1);
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  if (warp == 0) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tmem_cols(NB))
-                 : "memory");
-  }
+  fence_after_sync();
+  if (warp == GC_MMA_WARP) tmem_dealloc(tmem, TCOLS);
 }
 
-__global__ void tc_gram_reduce_kernel(const double* partial, int nsplit, int n, double* G) {
-  int e = blockIdx.x * blockDim.x + threadIdx.x;
+// one warp per Gram entry over its contiguous unit partials, fixed shuffle tree
+__global__ void tc_gram_reduce_kernel(const double2* __restrict__ partial, int nsplit, int n,
+                                      double2* __restrict__ G) {
+  const int e = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (e >= n) return;
+  const double2* p = partial + (long long)e * nsplit;
   double sr = 0.0, si = 0.0;
-  for (int s = 0; s < nsplit; ++s) {
-    sr += partial[((long long)s * n + e) * 2];
-    si += partial[((long long)s * n + e) * 2 + 1];
+  for (int s = lane; s < nsplit; s += 32) {
+    sr += p[s].x;
+    si += p[s].y;
   }
-  G[2 * e] = sr;
-  G[2 * e + 1] = si;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    sr += __shfl_xor_sync(0xffffffffu, sr, o);
+    si += __shfl_xor_sync(0xffffffffu, si, o);
+  }
+  if (lane == 0) G[e] = make_double2(sr, si);
 }
 
 int tc_nb(int mb) { return mb <= 16 ? 16 : (mb <= 32 ? 32 : 64); }
 
-int tc_splits(int ma, int mb, long long K) {
-  const int nb = tc_nb(mb);
-  long long tiles = (long long)((ma + 63) / 64) * ((mb + nb - 1) / nb);
-  long long target = (152 * 3) / (tiles > 0 ? tiles : 1);
-  if (target < 1) target = 1;
-  long long maxs = (K + 1023) / 1024;                   // >= 1024 complex per chunk
-  long long s = target < maxs ? target : maxs;
-  return (int)(s < 1 ? 1 : s);
+template <int NB>
+size_t gc_smem() {
+  constexpr int B_BYTES = 2 * NB * GC_KB * 4;
+  constexpr int OP_BYTES = 2 * GC_A_HALF + B_BYTES;
+  constexpr int IPT = ((64 + NB) * (GC_KB / 4) + GC_CONV - 1) / GC_CONV;
+  return (size_t)GC_NBUF * OP_BYTES + (size_t)GC_RAW * IPT * GC_CONV * 16;
+}
+
+int sm_count_dev() {
+  static int cached[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (cached[dev] == 0) {
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    cached[dev] = n > 0 ? n : 1;
+  }
+  return cached[dev];
+}
+
+struct GcPlan {
+  int mt, nb, nit, njt, nk;
+  long long kchunk;
+};
+
+GcPlan gc_plan(int ma, int mb, long long K) {
+  GcPlan p;
+  p.mt = ma <= 32 ? 32 : 64;
+  p.nb = tc_nb(mb);
+  p.nit = (ma + p.mt - 1) / p.mt;
+  p.njt = (mb + p.nb - 1) / p.nb;
+  const long long tiles = (long long)p.nit * p.njt;
+  const long long sms = sm_count_dev();
+  long long nk = (2 * sms + tiles - 1) / tiles;               // about two units per SM
+  const long long maxk = (K + 2047) / 2048;                   // >= 2048 complex per unit
+  if (nk > maxk) nk = maxk;
+  if (nk < 1) nk = 1;
+  long long kchunk = (K + nk - 1) / nk;
+  kchunk = (kchunk + 15) / 16 * 16;
+  p.kchunk = kchunk;
+  p.nk = (int)((K + kchunk - 1) / kchunk);
+  return p;
 }
 
 template <int NB>
-void launch_tc(dim3 grid, cudaStream_t st, const float* A, const float* B, int ma, int mb, long long K,
-               long long kchunk, double* part, int* err) {
-  const size_t smem = (size_t)2 * (2 * TC_M * TC_KB * 4 + 2 * NB * TC_KB * 4) + 1024;
+void launch_gc(const GcPlan& p, cudaStream_t st, const float* A, const float* B, int ma, int mb,
+               long long K, double* part, int* err) {
+  GcArgs a;
+  a.A = A;
+  a.B = B;
+  a.partial = part;
+  a.err = err;
+  a.K = K;
+  a.kchunk = p.kchunk;
+  a.ma = ma;
+  a.mb = mb;
+  a.mt = p.mt;
+  a.nit = p.nit;
+  a.njt = p.njt;
+  a.nk = p.nk;
+  const size_t smem = gc_smem<NB>();
   ef::set_smem_once(tc_gram_kernel<NB>, smem);
-  tc_gram_kernel<NB><<<grid, TC_THREADS, smem, st>>>(A, B, ma, mb, K, kchunk, part, err);
+  long long units = (long long)p.nit * p.njt * p.nk;
+  long long grid = sm_count_dev();
+  if (grid > units) grid = units;
+  tc_gram_kernel<NB><<<(unsigned)grid, GC_THREADS, smem, st>>>(a);
 }
 
 }  // namespace
 
 extern "C" size_t ef_gram_tc_workspace_bytes(int ma, int mb, long long K) {
   if (ma <= 0 || mb <= 0 || K <= 0) return 0;
-  return (size_t)tc_splits(ma, mb, K) * ma * mb * 2 * sizeof(double) + 512;
+  const GcPlan p = gc_plan(ma, mb, K);
+  return (size_t)p.nk * ma * mb * 2 * sizeof(double) + 512;
 }
 
 extern "C" int ef_gram_tc(const float* A, const float* B, int ma, int mb, long long K, double* G,
@@ -287,17 +428,12 @@ extern "C" int ef_gram_tc(const float* A, const float* B, int ma, int mb, long l
   if (!work || work_bytes < ef_gram_tc_workspace_bytes(ma, mb, K))
     return ef_fail(EF_ERR_WORKSPACE, "gram_tc work buffer too small");
   cudaStream_t st = (cudaStream_t)stream;
-  const int nb = tc_nb(mb);
-  int ns = tc_splits(ma, mb, K);
-  long long kchunk = (K + ns - 1) / ns;
-  kchunk = (kchunk + 15) / 16 * 16;
-  ns = (int)((K + kchunk - 1) / kchunk);
-  dim3 grid((ma + 63) / 64, (mb + nb - 1) / nb, ns);
+  const GcPlan p = gc_plan(ma, mb, K);
   ef_count_launches(2);
-  if (nb == 16) launch_tc<16>(grid, st, A, B, ma, mb, K, kchunk, (double*)work, err_dev);
-  else if (nb == 32) launch_tc<32>(grid, st, A, B, ma, mb, K, kchunk, (double*)work, err_dev);
-  else launch_tc<64>(grid, st, A, B, ma, mb, K, kchunk, (double*)work, err_dev);
-  int n = ma * mb;
-  tc_gram_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>((const double*)work, ns, n, G);
+  if (p.nb == 16) launch_gc<16>(p, st, A, B, ma, mb, K, (double*)work, err_dev);
+  else if (p.nb == 32) launch_gc<32>(p, st, A, B, ma, mb, K, (double*)work, err_dev);
+  else launch_gc<64>(p, st, A, B, ma, mb, K, (double*)work, err_dev);
+  const int n = ma * mb;
+  tc_gram_reduce_kernel<<<(n + 7) / 8, 256, 0, st>>>((const double2*)work, p.nk, n, (double2*)G);
   return ef_check_launch();
 }

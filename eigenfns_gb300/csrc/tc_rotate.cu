@@ -9,13 +9,13 @@
 // fp32-class accuracy: D += A_hi B_hi + A_hi B_lo + A_lo B_hi.
 //
 // Tiles are 128 real positions (M = 128 TMEM lanes); N = 2 * m_out padded to 8.
-// A persistent CTA (416 threads) walks its tiles with three warp roles:
-//   warps 0-7   convert: load S (one position per thread, 16 rows each of a
-//               32-row stage, two stages of loads in flight), split hi/lo, store
-//               16-byte quads into a 3-deep ring of K-major operand stages;
-//   warp 12     one thread issues the MMAs of each stage into one of two TMEM
+// A persistent CTA (288 threads) walks its tiles with three warp roles:
+//   warps 0-3   convert: one position per thread, the 16 rows of a stage through a
+//               private 8-deep cp.async ring, split hi/lo, store 16-byte quads into
+//               a 3-deep ring of K-major operand stages;
+//   warp 8      one thread issues the MMAs of each stage into one of two TMEM
 //               accumulators and commits them to the stage's "empty" barrier;
-//   warps 8-11  drain a finished accumulator (tcgen05.ld, one lane per thread),
+//   warps 4-7   drain a finished accumulator (tcgen05.ld, one lane per thread),
 //               combine D1/D2 with a lane exchange and store (set, add or subtract).
 // The coefficient operand [Re C | Im C] (hi and lo) is built once per CTA and stays
 // resident in shared memory. Every wait is bounded: on timeout the kernel sets the
@@ -33,17 +33,17 @@ namespace {
 
 using namespace ef::tc;
 
-constexpr int TR_THREADS = 416;
-constexpr int TR_CONV = 256;              // converter threads (warps 0-7)
-constexpr int TR_EPI0 = 256;              // first epilogue thread (warps 8-11)
-constexpr int TR_MMA_WARP = 12;
+constexpr int TR_THREADS = 288;
+constexpr int TR_CONV = 128;              // converter threads (warps 0-3)
+constexpr int TR_EPI0 = 128;              // first epilogue thread (warps 4-7)
+constexpr int TR_MMA_WARP = 8;
 constexpr int TR_M = 128;                 // real positions per tile
 constexpr int TR_JC = 16;                 // rows of S per stage
 constexpr int TR_NBUF = 3;                // operand stages in the ring
 constexpr int TR_OP_HALF = TR_M * TR_JC * 4;       // 8 KB: hi or lo of one stage
 constexpr int TR_OP_BYTES = 2 * TR_OP_HALF;        // 16 KB per stage
 constexpr int TR_RAW = 8;                 // raw stages in flight per converter thread
-constexpr int TR_ROWS_T = TR_JC / 2;      // rows per converter thread per stage
+constexpr int TR_ROWS_T = TR_JC;          // rows per converter thread per stage
 constexpr int TR_RAW_BYTES = TR_CONV * TR_ROWS_T * 4;   // 8 KB per raw stage
 constexpr int TR_SMEM_MAX = 227 * 1024 - 1024;   // dynamic part; static barriers take the rest
 
@@ -58,7 +58,8 @@ struct TrArgs {
   int ldc, m_in, m_out, mp, nch, mode;
 };
 
-__global__ void __maxnreg__(152) tc_rotate_kernel(const TrArgs a) {
+// 9 warps: at most 3 per SM sub-partition, so 168 registers a thread still fit
+__global__ void __maxnreg__(168) tc_rotate_kernel(const TrArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t op_full[TR_NBUF], op_empty[TR_NBUF];
   __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done_bar;
@@ -115,7 +116,7 @@ __global__ void __maxnreg__(152) tc_rotate_kernel(const TrArgs a) {
       (a.ntiles > blockIdx.x) ? (a.ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
   const long long nstages = my_tiles * a.nch;
 
-  if (warp < 8) {
+  if (warp < 4) {
     // ---------------- converters ----------------
     // Each thread owns one position p and TR_ROWS_T rows of every stage. Its values
     // travel through a private ring of TR_RAW raw stages (4-byte cp.async, zero-fill
@@ -173,7 +174,7 @@ __global__ void __maxnreg__(152) tc_rotate_kernel(const TrArgs a) {
       mbar_arrive(&op_full[o]);
     }
     asm volatile("cp.async.wait_group 0;" ::: "memory");
-  } else if (warp < 12) {
+  } else if (warp < 8) {
     // ---------------- epilogue ----------------
     // For the accumulate modes the current output values of the first 32 rows are
     // loaded before the wait for the accumulator, so their latency overlaps the MMAs.

@@ -288,3 +288,17 @@ def test_rotate_tensor_core_matches_cuda_core(gpu, m_in, m_out, monkeypatch):
     assert np.abs(tc.cpu().numpy() - ref).max() < 3e-6 * scale
     assert np.abs(simt.cpu().numpy() - ref).max() < 3e-6 * scale
     assert blas.tc_error() == 0
+
+
+@pytest.mark.parametrize("ma,mb,K", [(32, 32, 2 * 32 ** 3), (96, 96, 2 * 24 ** 3), (7, 45, 1002),
+                                     (200, 32, 2 * 16 ** 3), (64, 20, 2 * 20 ** 3 + 16)])
+def test_gram_tensor_core_matches_fp64(gpu, ma, mb, K):
+    """3xTF32 tcgen05 Gram with segment drains and fp64 unit reduction: fp32-class accuracy."""
+    from eigenfns_gb300 import blas
+    rng = np.random.default_rng(ma * 3 + mb)
+    A = (rng.standard_normal((ma, K)) + 1j * rng.standard_normal((ma, K))).astype(np.complex64)
+    B = (rng.standard_normal((mb, K)) + 1j * rng.standard_normal((mb, K))).astype(np.complex64)
+    got, err = blas.gram_tc(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda())
+    ref = A.astype(np.complex128).conj() @ B.astype(np.complex128).T
+    assert int(err.item()) == 0
+    assert np.abs(got.cpu().numpy() - ref).max() < 5e-6 * np.abs(ref).max()
