@@ -2,6 +2,7 @@
 
     python -m eigenfns_gb300.profile_kernels theta --grid 128 --m 2
     python -m eigenfns_gb300.profile_kernels gram --ma 32 --mb 32 --grid 128
+    python -m eigenfns_gb300.profile_kernels gram_tc --ma 32 --mb 32 --grid 128
     python -m eigenfns_gb300.profile_kernels rotate --ma 96 --mb 64 --grid 128
     python -m eigenfns_gb300.profile_kernels cheb --grid 192 --m 8 --steps 8
     python -m eigenfns_gb300.profile_kernels kpm --grid 256 --m 4 --steps 8
@@ -39,7 +40,7 @@ def _timed(fn, warm: int = 3) -> float:
 
 def main(argv=None) -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("kernel", choices=["theta", "precond", "gram", "rotate", "cheb", "kpm"])
+    ap.add_argument("kernel", choices=["theta", "precond", "gram", "gram_tc", "rotate", "cheb", "kpm"])
     ap.add_argument("--grid", type=int, default=128)
     ap.add_argument("--m", type=int, default=2)
     ap.add_argument("--ma", type=int, default=32)
@@ -71,6 +72,8 @@ def main(argv=None) -> None:
         B = torch.randn((a.mb, K), dtype=torch.complex64, device="cuda", generator=g)
         if a.kernel == "gram":
             ms = _timed(lambda: blas.gram(A, B))
+        elif a.kernel == "gram_tc":
+            ms = _timed(lambda: blas.gram_tc(A, B))
         else:
             C = np.random.default_rng(2).standard_normal((a.ma, a.mb)).astype(np.complex64)
             ms = _timed(lambda: blas.rotate(C, A, B))
