@@ -774,18 +774,20 @@ int ef_rotate(const float* C, const float* S, float* out, int m_in, int m_out, l
   cudaStream_t st = (cudaStream_t)stream;
   const char* kern = getenv("EF_ROTATE_KERNEL");
   const bool simt = kern && strcmp(kern, "simt") == 0;
-  if (!simt) {
-    // tensor cores: output groups of <= 64 columns, row chunks of what one pass holds
+  if (!simt && tiled) {
+    // tensor cores: output groups of <= 64 columns; a pass holds `cap` input rows, the
+    // accumulate modes spend m_out of them on the current output
     if (overlap) {
-      if (m_in <= ef::tc_rotate_max_rows(m_out))
+      if (m_in + (mode != 0 ? m_out : 0) <= ef::tc_rotate_max_rows(m_out))
         return ef::tc_rotate_launch(C, m_out, S, out, m_in, m_out, K, mode, st);
     } else {
       int rc = EF_OK;
       for (int i0 = 0; i0 < m_out && rc == EF_OK; i0 += 64) {
         const int mo = m_out - i0 < 64 ? m_out - i0 : 64;
-        const int rows = ef::tc_rotate_max_rows(mo);
-        for (int j0 = 0; j0 < m_in && rc == EF_OK; j0 += rows) {
-          const int mi = m_in - j0 < rows ? m_in - j0 : rows;
+        const int cap = ef::tc_rotate_max_rows(mo);
+        const int chunk = (mode == 0 && m_in <= cap) ? cap : cap - mo;
+        for (int j0 = 0; j0 < m_in && rc == EF_OK; j0 += chunk) {
+          const int mi = m_in - j0 < chunk ? m_in - j0 : chunk;
           const int md = j0 == 0 ? mode : (mode == 0 ? 1 : mode);
           rc = ef::tc_rotate_launch(C + 2 * ((long long)j0 * m_out + i0), m_out, S + 2 * (long long)j0 * K,
                                     out + 2 * (long long)i0 * K, mi, mo, K, md, st);

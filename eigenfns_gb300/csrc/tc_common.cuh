@@ -9,8 +9,10 @@
 namespace ef {
 namespace tc {
 
-// iterations of a bounded mbarrier wait (each try_wait may suspend briefly)
-constexpr unsigned long long kSpinLimit = 1ull << 26;
+// a bounded mbarrier wait gives up after this many nanoseconds of wall time
+constexpr unsigned long long kWaitLimitNs = 2000000000ull;
+// each try_wait may suspend the warp (off the issue slots) for up to this long
+constexpr uint32_t kSuspendHintNs = 1000000u;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -47,21 +49,32 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
       : "memory");
 }
 
-// waits for the phase of the given parity to complete; false after kSpinLimit tries
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// waits for the phase of the given parity to complete; the waiting warp is suspended
+// inside try_wait rather than spinning on the issue slots. Returns false once
+// kWaitLimitNs of wall time has passed without completion.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   const uint32_t a = smem_u32(bar);
-  for (unsigned long long it = 0; it < kSpinLimit; ++it) {
+  unsigned long long t0 = 0;
+  for (int it = 0;; ++it) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(a), "r"(parity)
+        : "r"(a), "r"(parity), "r"(kSuspendHintNs)
         : "memory");
     if (ok) return true;
+    const unsigned long long now = global_ns();
+    if (it == 0) t0 = now;
+    else if (now - t0 > kWaitLimitNs) return false;
   }
-  return false;
 }
 
 __device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,

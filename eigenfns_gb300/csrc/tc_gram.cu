@@ -15,12 +15,13 @@
 // registers while the next segment's MMAs run; a work unit's sum goes out in fp64
 // and units (K-chunks) are reduced in fp64.
 //
-// A persistent CTA (288 threads) walks work units (A-tile, B-tile, K-chunk):
-//   warps 0-3    converters: 16-byte cp.async of their (row, quad) items into a
-//                private 4-deep raw ring, hi/lo split (and the A' swap), 16-byte
-//                stores into a 3-deep ring of K-major operand stages;
-//   warp 8       one thread issues each stage's MMAs and commits them;
-//   warps 4-7    drain finished segments (one TMEM lane per thread, all columns)
+// A persistent CTA (416 threads) walks work units (A-tile, B-tile, K-chunk):
+//   warps 0-7    converters: 16-byte cp.async of each stage's rows into a 4-deep
+//                shared raw ring (a converter-only named barrier per stage), hi/lo
+//                split (and the A' swap), 16-byte stores into a 3-deep ring of
+//                K-major operand stages;
+//   warp 12      one thread issues each stage's MMAs and commits them;
+//   warps 8-11   drain finished segments (one TMEM lane per thread, all columns)
 //                and write the unit's partial sums.
 // Every mbarrier wait is bounded; on timeout the kernel sets the error flag, stops,
 // waits (bounded) for its own MMAs and frees its TMEM.
@@ -37,9 +38,10 @@ namespace {
 
 using namespace ef::tc;
 
-constexpr int GC_THREADS = 288;
-constexpr int GC_CONV = 128;          // converter threads (warps 0-3)
-constexpr int GC_MMA_WARP = 8;
+constexpr int GC_THREADS = 416;
+constexpr int GC_CONV = 256;          // converter threads (warps 0-7)
+constexpr int GC_MMA_WARP = 12;
+constexpr int GC_RAW_ROW = 144;       // raw ring row stride: 128 B of data + 16 B pad
 constexpr int GC_KB = 32;             // reals per stage (16 complex) = 4 k-steps of 8
 constexpr int GC_NBUF = 3;            // operand stages
 constexpr int GC_RAW = 4;             // raw stages per converter thread
@@ -66,13 +68,13 @@ struct GcArgs {
   int ma, mb, mt, nit, njt, nk;
 };
 
-// 9 warps: at most 3 per SM sub-partition, so 168 registers a thread still fit
+// 13 warps: at most 4 per SM sub-partition, so 128 registers a thread fit
 template <int NB>
-__global__ void __maxnreg__(168) tc_gram_kernel(const GcArgs a) {
+__global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a) {
   constexpr int B_BYTES = 2 * NB * GC_KB * 4;                  // [B_hi; B_lo]
   constexpr int OP_BYTES = 2 * GC_A_HALF + B_BYTES;
   constexpr int IPT = ((64 + NB) * (GC_KB / 4) + GC_CONV - 1) / GC_CONV;   // items per thread
-  constexpr int RAW_BYTES = IPT * GC_CONV * 16;
+  constexpr int RAW_BYTES = (64 + NB) * GC_RAW_ROW;
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t op_full[GC_NBUF], op_empty[GC_NBUF];
   __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done_bar;
@@ -122,11 +124,12 @@ __global__ void __maxnreg__(168) tc_gram_kernel(const GcArgs a) {
     nst = kend > kbeg ? (int)((kend - kbeg + GC_KB / 2 - 1) / (GC_KB / 2)) : 0;
   };
 
-  if (warp < 4) {
+  if (warp < 8) {
     // ---------------- converters ----------------
-    // item e of a stage: row r = e % (mt + NB), quad q = e / (mt + NB); rows [0, mt) are
-    // A rows, [mt, mt + NB) B rows. Consecutive threads take consecutive rows, so the
-    // 16-byte operand stores of 8 threads fill one 128-byte core-matrix line.
+    // copy: the stage's rows (A rows [0, mt), B rows [mt, mt + NB)) as 16-byte chunks,
+    // 8 per row, into a shared raw ring whose rows are padded to 144 B; convert: item
+    // e -> row r = e % rows, quad q = e / rows, so consecutive threads take consecutive
+    // rows and both the raw reads and the 16-byte operand stores are conflict-free.
     const int rows = a.mt + NB;
     long long s_issue = 0;
     long long ku = 0;                                // issue cursor: unit, stage in unit
@@ -139,18 +142,18 @@ __global__ void __maxnreg__(168) tc_gram_kernel(const GcArgs a) {
         st_in = 0;
         if (ku < my_units) unit_of(ku, it, jt, kc, kbeg, nst);
       }
-      if (ku < my_units) {
+      if (ku < my_units && !abort_s) {
         const int i0 = it * a.mt, j0 = jt * NB;
         const long long kc0 = kbeg + (long long)st_in * (GC_KB / 2);
         long long kend = kbeg + a.kchunk;
         if (kend > a.K) kend = a.K;
-        const uint32_t slot = smem_u32(raw + (int)(s_issue % GC_RAW) * RAW_BYTES) + tid * 16;
+        const uint32_t slot = smem_u32(raw + (int)(s_issue % GC_RAW) * RAW_BYTES);
 #pragma unroll
         for (int u = 0; u < IPT; ++u) {
-          const int e = tid + u * GC_CONV;
-          const int r = e % rows, q = e / rows;
-          const long long kq = kc0 + 2 * q;
-          bool in = e < nitems && kq < kend;
+          const int ch = tid + u * GC_CONV;
+          const int r = ch >> 3, c = ch & 7;
+          const long long kq = kc0 + 2 * c;
+          bool in = r < rows && kq < kend;
           const float* g = a.A;
           if (in) {
             if (r < a.mt) {
@@ -161,9 +164,12 @@ __global__ void __maxnreg__(168) tc_gram_kernel(const GcArgs a) {
               g = a.B + ((long long)(j0 + r - a.mt) * a.K + kq) * 2;
             }
           }
-          asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(slot + u * GC_CONV * 16),
-                       "l"(in ? g : a.A), "r"(in ? 16 : 0) : "memory");
+          if (r < rows)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(slot + r * GC_RAW_ROW + c * 16),
+                         "l"(in ? g : a.A), "r"(in ? 16 : 0) : "memory");
         }
+      }
+      if (ku < my_units) {
         ++st_in;
         ++s_issue;
       }
@@ -177,19 +183,25 @@ __global__ void __maxnreg__(168) tc_gram_kernel(const GcArgs a) {
       total += n1;
     }
     for (int s = 0; s < GC_RAW - 1; ++s) issue();
+    // every converter thread runs every iteration (named barrier counts stay uniform)
     for (long long s = 0; s < total; ++s) {
-      if (abort_s) break;
-      issue();
-      asm volatile("cp.async.wait_group %0;" ::"n"(GC_RAW - 1) : "memory");
-      const float4* rs = reinterpret_cast<const float4*>(raw + (int)(s % GC_RAW) * RAW_BYTES) + tid;
+      asm volatile("cp.async.wait_group %0;" ::"n"(GC_RAW - 2) : "memory");
+      asm volatile("bar.sync 1, %0;" ::"n"(GC_CONV) : "memory");
+      issue();                                      // refills the slot all threads finished reading
+      const unsigned char* rs = raw + (int)(s % GC_RAW) * RAW_BYTES;
       float4 v[IPT];
 #pragma unroll
-      for (int u = 0; u < IPT; ++u) v[u] = rs[u * GC_CONV];
+      for (int u = 0; u < IPT; ++u) {
+        const int e = tid + u * GC_CONV;
+        v[u] = e < nitems ? *reinterpret_cast<const float4*>(rs + (e % rows) * GC_RAW_ROW + (e / rows) * 16)
+                          : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
       const int o = (int)(s % GC_NBUF);
+      if (abort_s) continue;
       if (!mbar_wait(&op_empty[o], (uint32_t)(((s / GC_NBUF) + 1) & 1))) {
         abort_s = 1;
         atomicExch(a.err, 1);
-        break;
+        continue;
       }
       unsigned char* base = smem + o * OP_BYTES;
 #pragma unroll
@@ -219,7 +231,7 @@ __global__ void __maxnreg__(168) tc_gram_kernel(const GcArgs a) {
       mbar_arrive(&op_full[o]);
     }
     asm volatile("cp.async.wait_group 0;" ::: "memory");
-  } else if (warp < 8) {
+  } else if (warp < 12) {
     // ---------------- drain ----------------
     const int lq = warp & 3;
     const int L = lq * 32 + lane;                       // TMEM lane = M row
@@ -346,8 +358,7 @@ template <int NB>
 size_t gc_smem() {
   constexpr int B_BYTES = 2 * NB * GC_KB * 4;
   constexpr int OP_BYTES = 2 * GC_A_HALF + B_BYTES;
-  constexpr int IPT = ((64 + NB) * (GC_KB / 4) + GC_CONV - 1) / GC_CONV;
-  return (size_t)GC_NBUF * OP_BYTES + (size_t)GC_RAW * IPT * GC_CONV * 16;
+  return (size_t)GC_NBUF * OP_BYTES + (size_t)GC_RAW * (64 + NB) * GC_RAW_ROW;
 }
 
 int sm_count_dev() {

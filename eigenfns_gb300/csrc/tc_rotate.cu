@@ -7,20 +7,24 @@
 // followed by a neighbour exchange (adjacent TMEM lanes = adjacent threads of a warp)
 // gives the complex result. Three TF32 products per pair (x = hi + lo) give
 // fp32-class accuracy: D += A_hi B_hi + A_hi B_lo + A_lo B_hi.
+// The accumulate modes out (+/-)= ... fold the current output into the same GEMM:
+// its m_out rows are appended to S with identity coefficients and C is negated for
+// subtraction, so every mode ends in a plain store.
 //
 // Tiles are 128 real positions (M = 128 TMEM lanes); N = 2 * m_out padded to 8.
-// A persistent CTA (288 threads) walks its tiles with three warp roles:
-//   warps 0-3   convert: one position per thread, the 16 rows of a stage through a
-//               private 8-deep cp.async ring, split hi/lo, store 16-byte quads into
-//               a 3-deep ring of K-major operand stages;
-//   warp 8      one thread issues the MMAs of each stage into one of two TMEM
+// A persistent CTA (416 threads) walks its tiles with three warp roles:
+//   warps 0-7   convert: 16-byte cp.async of 16-row x 128-position stages into an
+//               8-deep shared raw ring (a converter-only named barrier per stage),
+//               split hi/lo, store 16-byte quads into a 3-deep ring of K-major
+//               operand stages;
+//   warp 12     one thread issues the MMAs of each stage into one of two TMEM
 //               accumulators and commits them to the stage's "empty" barrier;
-//   warps 4-7   drain a finished accumulator (tcgen05.ld, one lane per thread),
-//               combine D1/D2 with a lane exchange and store (set, add or subtract).
+//   warps 8-11  drain a finished accumulator (tcgen05.ld, one lane per thread),
+//               combine D1/D2 with a lane exchange and store.
 // The coefficient operand [Re C | Im C] (hi and lo) is built once per CTA and stays
-// resident in shared memory. Every wait is bounded: on timeout the kernel sets the
-// library's device error flag, stops issuing work, waits (bounded) for its own MMAs
-// and frees its TMEM.
+// resident in shared memory. Every mbarrier wait is bounded: on timeout the kernel
+// sets the library's device error flag and stops issuing work (the converters keep
+// their barrier count uniform), waits (bounded) for its own MMAs and frees its TMEM.
 //
 // Reference: tensordot(C.T, S) in combine / rotations, eigenfns/solver.py:49-57,106,125.
 #include <cstdint>
@@ -33,18 +37,17 @@ namespace {
 
 using namespace ef::tc;
 
-constexpr int TR_THREADS = 288;
-constexpr int TR_CONV = 128;              // converter threads (warps 0-3)
-constexpr int TR_EPI0 = 128;              // first epilogue thread (warps 4-7)
-constexpr int TR_MMA_WARP = 8;
+constexpr int TR_THREADS = 416;
+constexpr int TR_CONV = 256;              // converter threads (warps 0-7)
+constexpr int TR_EPI0 = 256;              // first epilogue thread (warps 8-11)
+constexpr int TR_MMA_WARP = 12;
 constexpr int TR_M = 128;                 // real positions per tile
 constexpr int TR_JC = 16;                 // rows of S per stage
 constexpr int TR_NBUF = 3;                // operand stages in the ring
 constexpr int TR_OP_HALF = TR_M * TR_JC * 4;       // 8 KB: hi or lo of one stage
 constexpr int TR_OP_BYTES = 2 * TR_OP_HALF;        // 16 KB per stage
-constexpr int TR_RAW = 8;                 // raw stages in flight per converter thread
-constexpr int TR_ROWS_T = TR_JC;          // rows per converter thread per stage
-constexpr int TR_RAW_BYTES = TR_CONV * TR_ROWS_T * 4;   // 8 KB per raw stage
+constexpr int TR_RAW = 8;                 // raw stages in flight
+constexpr int TR_RAW_BYTES = TR_JC * TR_M * 4;     // 8 KB per raw stage (row-major)
 constexpr int TR_SMEM_MAX = 227 * 1024 - 1024;   // dynamic part; static barriers take the rest
 
 __device__ int g_tc_error = 0;
@@ -52,14 +55,15 @@ __device__ int g_tc_error = 0;
 struct TrArgs {
   const float2* C;      // (m_in, ldc) complex, columns [0, m_out) used
   const float* S;       // m_in rows of n2 floats
-  float* out;           // m_out rows of n2 floats
+  float* out;           // m_out rows of n2 floats (also the identity rows when mode != 0)
   long long n2;         // 2K
   long long ntiles;
-  int ldc, m_in, m_out, mp, nch, mode;
+  int ldc, m_in, m_tot, m_out, mp, nch;
+  float sign;           // -1 for subtraction
 };
 
-// 9 warps: at most 3 per SM sub-partition, so 168 registers a thread still fit
-__global__ void __maxnreg__(168) tc_rotate_kernel(const TrArgs a) {
+// 13 warps: at most 4 per SM sub-partition, so 128 registers a thread fit
+__global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t op_full[TR_NBUF], op_empty[TR_NBUF];
   __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done_bar;
@@ -88,24 +92,25 @@ __global__ void __maxnreg__(168) tc_rotate_kernel(const TrArgs a) {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   // coefficient operand, K-major core matrices: row n (D column), column j (row of S)
-  // rows [0, mp) = Re C[:, n], rows [mp, 2mp) = Im C[:, n - mp]; zero padding elsewhere
+  // rows [0, mp) = Re C[:, n], rows [mp, 2mp) = Im C[:, n - mp]; rows j >= m_in of
+  // the inputs are the current output (identity coefficients); zero padding elsewhere
   for (int e = tid; e < (int)(2 * b_half / 16); e += TR_THREADS)
     reinterpret_cast<float4*>(bops)[e] = make_float4(0.f, 0.f, 0.f, 0.f);
   __syncthreads();
   const int kq = kj / 4;
+  auto put = [&](int n, int j, float x) {
+    const float hi = tf32_rn(x), lo = tf32_rn(x - hi);
+    const uint32_t off = (uint32_t)(((n >> 3) * kq + (j >> 2)) * 128 + (n & 7) * 16 + (j & 3) * 4);
+    *reinterpret_cast<float*>(bops + off) = hi;
+    *reinterpret_cast<float*>(bops + b_half + off) = lo;
+  };
   for (int e = tid; e < a.m_in * a.m_out; e += TR_THREADS) {
     const int j = e / a.m_out, i = e - j * a.m_out;
     const float2 c = a.C[(long long)j * a.ldc + i];
-#pragma unroll
-    for (int part = 0; part < 2; ++part) {
-      const int n = part ? a.mp + i : i;
-      const float x = part ? c.y : c.x;
-      const float hi = tf32_rn(x), lo = tf32_rn(x - hi);
-      const uint32_t off = (uint32_t)(((n >> 3) * kq + (j >> 2)) * 128 + (n & 7) * 16 + (j & 3) * 4);
-      *reinterpret_cast<float*>(bops + off) = hi;
-      *reinterpret_cast<float*>(bops + b_half + off) = lo;
-    }
+    put(i, j, a.sign * c.x);
+    put(a.mp + i, j, a.sign * c.y);
   }
+  for (int i = tid; i < a.m_tot - a.m_in; i += TR_THREADS) put(i, a.m_in + i, 1.f);
   fence_async_smem();
   if (warp == TR_MMA_WARP) tmem_alloc(&tmem_base_s, tcols);
   fence_before_sync();
@@ -116,52 +121,56 @@ __global__ void __maxnreg__(168) tc_rotate_kernel(const TrArgs a) {
       (a.ntiles > blockIdx.x) ? (a.ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
   const long long nstages = my_tiles * a.nch;
 
-  if (warp < 4) {
+  if (warp < 8) {
     // ---------------- converters ----------------
-    // Each thread owns one position p and TR_ROWS_T rows of every stage. Its values
-    // travel through a private ring of TR_RAW raw stages (4-byte cp.async, zero-fill
-    // outside the matrix), so TR_RAW stages of loads are in flight without holding
-    // registers; the thread then splits hi/lo and stores 16-byte quads.
+    // copy: 16 rows x 32 chunks of 16 B per stage, two chunks per thread; convert: each
+    // thread owns position p and rows 8h..8h+7 of the stage (conflict-free reads).
     const int p = tid & (TR_M - 1), h = tid >> 7;
     auto issue = [&](long long s) {
-      if (s < nstages) {
+      if (s < nstages && !abort_s) {
         const long long tile = blockIdx.x + (s / a.nch) * (long long)gridDim.x;
         const int c = (int)(s % a.nch);
-        const long long pos = tile * TR_M + p;
-        const int j0 = c * TR_JC + h * TR_ROWS_T;
-        const bool pin = pos < a.n2;
-        const uint32_t slot = smem_u32(raw + (int)(s % TR_RAW) * TR_RAW_BYTES) + tid * 4;
+        const uint32_t slot = smem_u32(raw + (int)(s % TR_RAW) * TR_RAW_BYTES);
 #pragma unroll
-        for (int r = 0; r < TR_ROWS_T; ++r) {
-          const int j = j0 + r;
-          const bool in = pin && j < a.m_in;
-          const float* g = a.S + (in ? (long long)j * a.n2 + pos : 0);
-          asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(slot + r * TR_CONV * 4),
-                       "l"(g), "r"(in ? 4 : 0) : "memory");
+        for (int k = 0; k < 2; ++k) {
+          const int ch = tid + k * TR_CONV;
+          const int row = ch >> 5, c16 = ch & 31;
+          const int j = c * TR_JC + row;
+          const long long pos = tile * TR_M + c16 * 4;
+          const bool in = j < a.m_tot && pos < a.n2;
+          const float* g = a.S;
+          if (in)
+            g = (j < a.m_in) ? a.S + (long long)j * a.n2 + pos
+                             : a.out + (long long)(j - a.m_in) * a.n2 + pos;
+          asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
+                       ::"r"(slot + row * (TR_M * 4) + c16 * 16), "l"(g), "r"(in ? 16 : 0)
+                       : "memory");
         }
       }
       asm volatile("cp.async.commit_group;" ::: "memory");
     };
     for (long long s = 0; s < TR_RAW - 1; ++s) issue(s);
+    // every converter thread runs every iteration (named barrier counts stay uniform)
     for (long long s = 0; s < nstages; ++s) {
-      if (abort_s) break;
-      issue(s + TR_RAW - 1);
-      asm volatile("cp.async.wait_group %0;" ::"n"(TR_RAW - 1) : "memory");
-      const float* rs = reinterpret_cast<const float*>(raw + (int)(s % TR_RAW) * TR_RAW_BYTES) + tid;
-      float v[TR_ROWS_T];
+      asm volatile("cp.async.wait_group %0;" ::"n"(TR_RAW - 2) : "memory");
+      asm volatile("bar.sync 1, %0;" ::"n"(TR_CONV) : "memory");
+      issue(s + TR_RAW - 1);                 // refills the slot every thread finished reading
+      const float* rs = reinterpret_cast<const float*>(raw + (int)(s % TR_RAW) * TR_RAW_BYTES) + p;
+      float v[8];
 #pragma unroll
-      for (int r = 0; r < TR_ROWS_T; ++r) v[r] = rs[r * TR_CONV];
+      for (int r = 0; r < 8; ++r) v[r] = rs[(h * 8 + r) * TR_M];
       const int o = (int)(s % TR_NBUF);
       const uint32_t u = (uint32_t)(s / TR_NBUF);
+      if (abort_s) continue;
       if (!mbar_wait(&op_empty[o], (u + 1) & 1)) {
         abort_s = 1;
         atomicExch(&g_tc_error, 1);
-        break;
+        continue;
       }
       unsigned char* base = smem + o * TR_OP_BYTES;
 #pragma unroll
-      for (int qq = 0; qq < TR_ROWS_T / 4; ++qq) {
-        const int q = h * (TR_ROWS_T / 4) + qq;
+      for (int qq = 0; qq < 2; ++qq) {
+        const int q = h * 2 + qq;
         const float4 x = make_float4(v[4 * qq], v[4 * qq + 1], v[4 * qq + 2], v[4 * qq + 3]);
         const float4 hi = make_float4(tf32_rn(x.x), tf32_rn(x.y), tf32_rn(x.z), tf32_rn(x.w));
         const float4 lo = make_float4(tf32_rn(x.x - hi.x), tf32_rn(x.y - hi.y), tf32_rn(x.z - hi.z),
@@ -174,61 +183,33 @@ __global__ void __maxnreg__(168) tc_rotate_kernel(const TrArgs a) {
       mbar_arrive(&op_full[o]);
     }
     asm volatile("cp.async.wait_group 0;" ::: "memory");
-  } else if (warp < 8) {
+  } else if (warp < 12) {
     // ---------------- epilogue ----------------
-    // For the accumulate modes the current output values of the first 32 rows are
-    // loaded before the wait for the accumulator, so their latency overlaps the MMAs.
     const int p = tid - TR_EPI0;                       // = 32 * (warp % 4) + lane
     const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
     const bool even = (p & 1) == 0;
     for (long long k = 0; k < my_tiles; ++k) {
       if (abort_s) break;
       const int ab = (int)(k & 1);
-      const long long tile = blockIdx.x + k * (long long)gridDim.x;
-      const long long pos = tile * TR_M + p;
-      const bool pin = pos < a.n2;
-      float prev[32];
-#pragma unroll
-      for (int t = 0; t < 32; ++t)
-        prev[t] = (a.mode != 0 && pin && t < a.m_out) ? a.out[(long long)t * a.n2 + pos] : 0.f;
       if (!mbar_wait(&acc_full[ab], (uint32_t)((k >> 1) & 1))) {
         abort_s = 1;
         atomicExch(&g_tc_error, 1);
         break;
       }
       fence_after_sync();
+      const long long tile = blockIdx.x + k * (long long)gridDim.x;
+      const long long pos = tile * TR_M + p;
+      const bool pin = pos < a.n2;
       const uint32_t ta = lane_base + (uint32_t)(ab * N);
-      auto emit = [&](int i0, const float (&pv)[8]) {
+      for (int i0 = 0; i0 < a.mp; i0 += 8) {
         float d1[8], d2[8];
         tmem_ld8x2(ta + i0, ta + a.mp + i0, d1, d2);
 #pragma unroll
         for (int t = 0; t < 8; ++t) {
           const float w = __shfl_xor_sync(0xffffffffu, d2[t], 1);
           const float val = even ? d1[t] - w : d1[t] + w;
-          const int i = i0 + t;
-          if (pin && i < a.m_out) {
-            float* o = a.out + (long long)i * a.n2 + pos;
-            if (a.mode == 0) *o = val;
-            else if (a.mode > 0) *o = pv[t] + val;
-            else *o = pv[t] - val;
-          }
+          if (pin && i0 + t < a.m_out) a.out[(long long)(i0 + t) * a.n2 + pos] = val;
         }
-      };
-#pragma unroll
-      for (int c8 = 0; c8 < 4; ++c8) {          // rows 0..31: prefetched values
-        if (c8 * 8 < a.mp) {
-          float pv[8];
-#pragma unroll
-          for (int t = 0; t < 8; ++t) pv[t] = prev[c8 * 8 + t];
-          emit(c8 * 8, pv);
-        }
-      }
-      for (int i0 = 32; i0 < a.mp; i0 += 8) {  // rows 32..63
-        float pv[8];
-#pragma unroll
-        for (int t = 0; t < 8; ++t)
-          pv[t] = (a.mode != 0 && pin && i0 + t < a.m_out) ? a.out[(long long)(i0 + t) * a.n2 + pos] : 0.f;
-        emit(i0, pv);
       }
       fence_before_sync();
       mbar_arrive(&acc_empty[ab]);
@@ -260,7 +241,7 @@ __global__ void __maxnreg__(168) tc_rotate_kernel(const TrArgs a) {
         const uint32_t a_hi = smem_u32(smem + o * TR_OP_BYTES), a_lo = a_hi + TR_OP_HALF;
 #pragma unroll
         for (int g = 0; g < TR_JC / 8; ++g) {
-          if (c * TR_JC + g * 8 >= a.m_in) break;      // all-zero rows: nothing to add
+          if (c * TR_JC + g * 8 >= a.m_tot) break;      // all-zero rows: nothing to add
           const uint64_t ah = smem_desc(a_hi + g * 256, 128, (TR_JC / 4) * 128);
           const uint64_t al = smem_desc(a_lo + g * 256, 128, (TR_JC / 4) * 128);
           const uint32_t boff = (uint32_t)(c * (TR_JC / 4) + 2 * g) * 128;
@@ -301,8 +282,8 @@ int sm_count() {
   return cached[dev];
 }
 
-size_t tr_smem(int m_in, int mp) {
-  const int nch = (m_in + TR_JC - 1) / TR_JC;
+size_t tr_smem(int m_tot, int mp) {
+  const int nch = (m_tot + TR_JC - 1) / TR_JC;
   return (size_t)TR_NBUF * TR_OP_BYTES + (size_t)TR_RAW * TR_RAW_BYTES +
          (size_t)2 * (2 * mp) * (nch * TR_JC) * 4;
 }
@@ -311,7 +292,8 @@ size_t tr_smem(int m_in, int mp) {
 
 namespace ef {
 
-// largest m_in one tensor-core pass takes for m_out outputs (0 when m_out > 64)
+// largest number of input rows (S rows plus, in the accumulate modes, the m_out
+// output rows) one tensor-core pass holds for m_out outputs; 0 when m_out > 64
 int tc_rotate_max_rows(int m_out) {
   if (m_out <= 0 || m_out > 64) return 0;
   const int mp = (m_out + 7) / 8 * 8;
@@ -320,7 +302,8 @@ int tc_rotate_max_rows(int m_out) {
   return rows;
 }
 
-// one pass: m_out <= 64, m_in <= tc_rotate_max_rows(m_out)
+// one pass: m_out <= 64, m_in + (mode ? m_out : 0) <= tc_rotate_max_rows(m_out);
+// S and out 16-byte aligned, K even
 int tc_rotate_launch(const float* C, int ldc, const float* S, float* out, int m_in, int m_out,
                      long long K, int mode, cudaStream_t st) {
   TrArgs a;
@@ -332,10 +315,11 @@ int tc_rotate_launch(const float* C, int ldc, const float* S, float* out, int m_
   a.ldc = ldc;
   a.m_in = m_in;
   a.m_out = m_out;
+  a.m_tot = m_in + (mode != 0 ? m_out : 0);
   a.mp = (m_out + 7) / 8 * 8;
-  a.nch = (m_in + TR_JC - 1) / TR_JC;
-  a.mode = mode;
-  const size_t smem = tr_smem(m_in, a.mp);
+  a.nch = (a.m_tot + TR_JC - 1) / TR_JC;
+  a.sign = mode < 0 ? -1.f : 1.f;
+  const size_t smem = tr_smem(a.m_tot, a.mp);
   ef::set_smem_once(tc_rotate_kernel, smem);
   long long grid = sm_count();
   if (grid > a.ntiles) grid = a.ntiles;
