@@ -131,6 +131,14 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a) {
     // e -> row r = e % rows, quad q = e / rows, so consecutive threads take consecutive
     // rows and both the raw reads and the 16-byte operand stores are conflict-free.
     const int rows = a.mt + NB;
+    // per-thread item geometry is stage-independent: computed once
+    int cr[IPT], cq[IPT];
+#pragma unroll
+    for (int u = 0; u < IPT; ++u) {
+      const int e = tid + u * GC_CONV;
+      cr[u] = e % rows;
+      cq[u] = e / rows;
+    }
     long long s_issue = 0;
     long long ku = 0;                                // issue cursor: unit, stage in unit
     int it = 0, jt = 0, kc = 0, nst = 0, st_in = 0;
@@ -193,7 +201,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a) {
 #pragma unroll
       for (int u = 0; u < IPT; ++u) {
         const int e = tid + u * GC_CONV;
-        v[u] = e < nitems ? *reinterpret_cast<const float4*>(rs + (e % rows) * GC_RAW_ROW + (e / rows) * 16)
+        v[u] = e < nitems ? *reinterpret_cast<const float4*>(rs + cr[u] * GC_RAW_ROW + cq[u] * 16)
                           : make_float4(0.f, 0.f, 0.f, 0.f);
       }
       const int o = (int)(s % GC_NBUF);
@@ -208,7 +216,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a) {
       for (int u = 0; u < IPT; ++u) {
         const int e = tid + u * GC_CONV;
         if (e < nitems) {
-          const int r = e % rows, q = e / rows;
+          const int r = cr[u], q = cq[u];
           const float4 x = v[u];
           const float4 h = make_float4(tf32_rn(x.x), tf32_rn(x.y), tf32_rn(x.z), tf32_rn(x.w));
           const float4 l = make_float4(tf32_rn(x.x - h.x), tf32_rn(x.y - h.y), tf32_rn(x.z - h.z),

@@ -46,7 +46,7 @@ constexpr int TR_JC = 16;                 // rows of S per stage
 constexpr int TR_NBUF = 3;                // operand stages in the ring
 constexpr int TR_OP_HALF = TR_M * TR_JC * 4;       // 8 KB: hi or lo of one stage
 constexpr int TR_OP_BYTES = 2 * TR_OP_HALF;        // 16 KB per stage
-constexpr int TR_RAW = 8;                 // raw stages in flight
+constexpr int TR_RAW = 8;                 // raw stages in flight (power of two)
 constexpr int TR_RAW_BYTES = TR_JC * TR_M * 4;     // 8 KB per raw stage (row-major)
 constexpr int TR_SMEM_MAX = 227 * 1024 - 1024;   // dynamic part; static barriers take the rest
 
@@ -126,26 +126,36 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a) {
     // copy: 16 rows x 32 chunks of 16 B per stage, two chunks per thread; convert: each
     // thread owns position p and rows 8h..8h+7 of the stage (conflict-free reads).
     const int p = tid & (TR_M - 1), h = tid >> 7;
+    // per-thread copy geometry is stage-independent; the issue cursor (tile, chunk)
+    // advances incrementally (no 64-bit division in the loop)
+    int row_k[2], c16_k[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      row_k[k] = (tid + k * TR_CONV) >> 5;
+      c16_k[k] = (tid + k * TR_CONV) & 31;
+    }
+    long long iss_tile = blockIdx.x;
+    int iss_c = 0;
     auto issue = [&](long long s) {
       if (s < nstages && !abort_s) {
-        const long long tile = blockIdx.x + (s / a.nch) * (long long)gridDim.x;
-        const int c = (int)(s % a.nch);
-        const uint32_t slot = smem_u32(raw + (int)(s % TR_RAW) * TR_RAW_BYTES);
+        const uint32_t slot = smem_u32(raw + (int)(s & (TR_RAW - 1)) * TR_RAW_BYTES);
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
-          const int ch = tid + k * TR_CONV;
-          const int row = ch >> 5, c16 = ch & 31;
-          const int j = c * TR_JC + row;
-          const long long pos = tile * TR_M + c16 * 4;
+          const int j = iss_c * TR_JC + row_k[k];
+          const long long pos = iss_tile * TR_M + c16_k[k] * 4;
           const bool in = j < a.m_tot && pos < a.n2;
           const float* g = a.S;
           if (in)
             g = (j < a.m_in) ? a.S + (long long)j * a.n2 + pos
                              : a.out + (long long)(j - a.m_in) * a.n2 + pos;
           asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
-                       ::"r"(slot + row * (TR_M * 4) + c16 * 16), "l"(g), "r"(in ? 16 : 0)
+                       ::"r"(slot + row_k[k] * (TR_M * 4) + c16_k[k] * 16), "l"(g), "r"(in ? 16 : 0)
                        : "memory");
         }
+      }
+      if (s < nstages && ++iss_c == a.nch) {
+        iss_c = 0;
+        iss_tile += gridDim.x;
       }
       asm volatile("cp.async.commit_group;" ::: "memory");
     };
@@ -155,7 +165,7 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a) {
       asm volatile("cp.async.wait_group %0;" ::"n"(TR_RAW - 2) : "memory");
       asm volatile("bar.sync 1, %0;" ::"n"(TR_CONV) : "memory");
       issue(s + TR_RAW - 1);                 // refills the slot every thread finished reading
-      const float* rs = reinterpret_cast<const float*>(raw + (int)(s % TR_RAW) * TR_RAW_BYTES) + p;
+      const float* rs = reinterpret_cast<const float*>(raw + (int)(s & (TR_RAW - 1)) * TR_RAW_BYTES) + p;
       float v[8];
 #pragma unroll
       for (int r = 0; r < 8; ++r) v[r] = rs[(h * 8 + r) * TR_M];
