@@ -290,6 +290,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a) {
   } else if (warp == GC_MMA_WARP && lane == 0) {
     // ---------------- MMA issue ----------------
     const uint32_t id1 = idesc_tf32(128, 2 * NB), id2 = idesc_tf32(128, NB);
+    const uint64_t desc0 = gram_desc(smem_u32(smem));
     long long s = 0, q = 0;
     bool issued = false;
     for (long long k = 0; k < my_units && !abort_s; ++k) {
@@ -313,13 +314,14 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a) {
         }
         fence_after_sync();
         const uint32_t d = tmem + (uint32_t)(ab * 2 * NB);
-        const uint32_t aHi = smem_u32(smem + o * OP_BYTES), aLo = aHi + GC_A_HALF;
-        const uint32_t bB = aHi + 2 * GC_A_HALF;
+        // descriptors differ from the base one only in the start-address field
+        const uint64_t aHi = desc0 + (uint64_t)((o * OP_BYTES) >> 4);
+        const uint64_t aLo = aHi + (uint64_t)(GC_A_HALF >> 4), bB = aHi + (uint64_t)((2 * GC_A_HALF) >> 4);
 #pragma unroll
         for (int g = 0; g < GC_KB / 8; ++g) {
-          const uint32_t off = g * 256;
-          mma_tf32(d, gram_desc(aHi + off), gram_desc(bB + off), id1, (seg_first && g == 0) ? 0u : 1u);
-          mma_tf32(d + NB, gram_desc(aLo + off), gram_desc(bB + off), id2, 1u);
+          const uint64_t off = (uint64_t)(g * 256 >> 4);
+          mma_tf32(d, aHi + off, bB + off, id1, (seg_first && g == 0) ? 0u : 1u);
+          mma_tf32(d + NB, aLo + off, bB + off, id2, 1u);
         }
         mma_commit(&op_empty[o]);
         issued = true;

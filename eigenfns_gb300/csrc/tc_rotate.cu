@@ -12,19 +12,19 @@
 // subtraction, so every mode ends in a plain store.
 //
 // Tiles are 128 real positions (M = 128 TMEM lanes); N = 2 * m_out padded to 8.
-// A persistent CTA (416 threads) walks its tiles with three warp roles:
-//   warps 0-7   convert: 16-byte cp.async of 16-row x 128-position stages into an
-//               8-deep shared raw ring (a converter-only named barrier per stage),
-//               split hi/lo, store 16-byte quads into a 3-deep ring of K-major
-//               operand stages;
+// A persistent CTA (448 threads) walks its tiles with four warp roles:
+//   warp 13     loads: one bulk copy (TMA engine) per 512-byte row of a 16-row x
+//               128-position stage into an 8-deep raw ring (mbarrier byte counts);
+//   warps 0-7   convert: read the raw stage (one position per thread), split hi/lo,
+//               store 16-byte quads into a 3-deep ring of K-major operand stages;
 //   warp 12     one thread issues the MMAs of each stage into one of two TMEM
 //               accumulators and commits them to the stage's "empty" barrier;
 //   warps 8-11  drain a finished accumulator (tcgen05.ld, one lane per thread),
 //               combine D1/D2 with a lane exchange and store.
 // The coefficient operand [Re C | Im C] (hi and lo) is built once per CTA and stays
 // resident in shared memory. Every mbarrier wait is bounded: on timeout the kernel
-// sets the library's device error flag and stops issuing work (the converters keep
-// their barrier count uniform), waits (bounded) for its own MMAs and frees its TMEM.
+// sets the library's device error flag and stops issuing work, waits (bounded) for
+// its own copies and MMAs and frees its TMEM.
 //
 // Reference: tensordot(C.T, S) in combine / rotations, eigenfns/solver.py:49-57,106,125.
 #include <cstdint>
@@ -37,10 +37,11 @@ namespace {
 
 using namespace ef::tc;
 
-constexpr int TR_THREADS = 416;
+constexpr int TR_THREADS = 448;
 constexpr int TR_CONV = 256;              // converter threads (warps 0-7)
 constexpr int TR_EPI0 = 256;              // first epilogue thread (warps 8-11)
 constexpr int TR_MMA_WARP = 12;
+constexpr int TR_LOAD_WARP = 13;
 constexpr int TR_M = 128;                 // real positions per tile
 constexpr int TR_JC = 16;                 // rows of S per stage
 constexpr int TR_NBUF = 3;                // operand stages in the ring
@@ -62,11 +63,12 @@ struct TrArgs {
   float sign;           // -1 for subtraction
 };
 
-// 13 warps: at most 4 per SM sub-partition, so 128 registers a thread fit
+// 14 warps: at most 4 per SM sub-partition, so 128 registers a thread fit
 __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t op_full[TR_NBUF], op_empty[TR_NBUF];
   __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done_bar;
+  __shared__ __align__(8) uint64_t raw_full[TR_RAW], raw_empty[TR_RAW];
   __shared__ uint32_t tmem_base_s;
   __shared__ volatile int abort_s;
 
@@ -89,6 +91,10 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a) {
       mbar_init(&acc_empty[b], 128);
     }
     mbar_init(&done_bar, 1);
+    for (int b = 0; b < TR_RAW; ++b) {
+      mbar_init(&raw_full[b], 1);
+      mbar_init(&raw_empty[b], TR_CONV);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   // coefficient operand, K-major core matrices: row n (D column), column j (row of S)
@@ -123,59 +129,36 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a) {
 
   if (warp < 8) {
     // ---------------- converters ----------------
-    // copy: 16 rows x 32 chunks of 16 B per stage, two chunks per thread; convert: each
-    // thread owns position p and rows 8h..8h+7 of the stage (conflict-free reads).
+    // each thread owns position p and rows 8h..8h+7 of a stage (conflict-free reads)
     const int p = tid & (TR_M - 1), h = tid >> 7;
-    // per-thread copy geometry is stage-independent; the issue cursor (tile, chunk)
-    // advances incrementally (no 64-bit division in the loop)
-    int row_k[2], c16_k[2];
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      row_k[k] = (tid + k * TR_CONV) >> 5;
-      c16_k[k] = (tid + k * TR_CONV) & 31;
-    }
-    long long iss_tile = blockIdx.x;
-    int iss_c = 0;
-    auto issue = [&](long long s) {
-      if (s < nstages && !abort_s) {
-        const uint32_t slot = smem_u32(raw + (int)(s & (TR_RAW - 1)) * TR_RAW_BYTES);
-#pragma unroll
-        for (int k = 0; k < 2; ++k) {
-          const int j = iss_c * TR_JC + row_k[k];
-          const long long pos = iss_tile * TR_M + c16_k[k] * 4;
-          const bool in = j < a.m_tot && pos < a.n2;
-          const float* g = a.S;
-          if (in)
-            g = (j < a.m_in) ? a.S + (long long)j * a.n2 + pos
-                             : a.out + (long long)(j - a.m_in) * a.n2 + pos;
-          asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
-                       ::"r"(slot + row_k[k] * (TR_M * 4) + c16_k[k] * 16), "l"(g), "r"(in ? 16 : 0)
-                       : "memory");
-        }
-      }
-      if (s < nstages && ++iss_c == a.nch) {
-        iss_c = 0;
-        iss_tile += gridDim.x;
-      }
-      asm volatile("cp.async.commit_group;" ::: "memory");
-    };
-    for (long long s = 0; s < TR_RAW - 1; ++s) issue(s);
-    // every converter thread runs every iteration (named barrier counts stay uniform)
+    long long cur_tile = blockIdx.x;
+    int cur_c = 0;
     for (long long s = 0; s < nstages; ++s) {
-      asm volatile("cp.async.wait_group %0;" ::"n"(TR_RAW - 2) : "memory");
-      asm volatile("bar.sync 1, %0;" ::"n"(TR_CONV) : "memory");
-      issue(s + TR_RAW - 1);                 // refills the slot every thread finished reading
-      const float* rs = reinterpret_cast<const float*>(raw + (int)(s & (TR_RAW - 1)) * TR_RAW_BYTES) + p;
+      const int slot = (int)(s & (TR_RAW - 1));
+      const uint32_t ur = (uint32_t)(s / TR_RAW);
+      if (abort_s) break;
+      if (!mbar_wait(&raw_full[slot], ur & 1)) {
+        abort_s = 1;
+        atomicExch(&g_tc_error, 1);
+        break;
+      }
+      const float* rs = reinterpret_cast<const float*>(raw + slot * TR_RAW_BYTES) + p;
+      const bool pin = cur_tile * TR_M + p < a.n2;
+      const int j0 = cur_c * TR_JC + h * 8;
       float v[8];
 #pragma unroll
-      for (int r = 0; r < 8; ++r) v[r] = rs[(h * 8 + r) * TR_M];
+      for (int r = 0; r < 8; ++r) v[r] = (pin && j0 + r < a.m_tot) ? rs[(h * 8 + r) * TR_M] : 0.f;
+      mbar_arrive(&raw_empty[slot]);
+      if (++cur_c == a.nch) {
+        cur_c = 0;
+        cur_tile += gridDim.x;
+      }
       const int o = (int)(s % TR_NBUF);
       const uint32_t u = (uint32_t)(s / TR_NBUF);
-      if (abort_s) continue;
       if (!mbar_wait(&op_empty[o], (u + 1) & 1)) {
         abort_s = 1;
         atomicExch(&g_tc_error, 1);
-        continue;
+        break;
       }
       unsigned char* base = smem + o * TR_OP_BYTES;
 #pragma unroll
@@ -192,7 +175,6 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a) {
       fence_async_smem();
       mbar_arrive(&op_full[o]);
     }
-    asm volatile("cp.async.wait_group 0;" ::: "memory");
   } else if (warp < 12) {
     // ---------------- epilogue ----------------
     const int p = tid - TR_EPI0;                       // = 32 * (warp % 4) + lane
@@ -227,8 +209,10 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a) {
   } else if (warp == TR_MMA_WARP && lane == 0) {
     // ---------------- MMA issue ----------------
     const uint32_t idesc = idesc_tf32(TR_M, N);
-    const uint32_t b_hi = smem_u32(bops), b_lo = b_hi + b_half;
+    const uint32_t b_hi = smem_u32(bops);
     const uint32_t b_sbo = (uint32_t)kq * 128;
+    const uint64_t a_desc0 = smem_desc(smem_u32(smem), 128, (TR_JC / 4) * 128);
+    const uint64_t b_desc0 = smem_desc(b_hi, 128, b_sbo);
     bool issued = false;
     for (long long k = 0; k < my_tiles && !abort_s; ++k) {
       const int ab = (int)(k & 1);
@@ -248,15 +232,14 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a) {
           break;
         }
         fence_after_sync();
-        const uint32_t a_hi = smem_u32(smem + o * TR_OP_BYTES), a_lo = a_hi + TR_OP_HALF;
+        // descriptors differ from the base ones only in the start-address field
+        const uint64_t ah0 = a_desc0 + (uint64_t)((o * TR_OP_BYTES) >> 4);
+        const uint64_t bh0 = b_desc0 + (uint64_t)((c * (TR_JC / 4) * 128) >> 4);
 #pragma unroll
         for (int g = 0; g < TR_JC / 8; ++g) {
           if (c * TR_JC + g * 8 >= a.m_tot) break;      // all-zero rows: nothing to add
-          const uint64_t ah = smem_desc(a_hi + g * 256, 128, (TR_JC / 4) * 128);
-          const uint64_t al = smem_desc(a_lo + g * 256, 128, (TR_JC / 4) * 128);
-          const uint32_t boff = (uint32_t)(c * (TR_JC / 4) + 2 * g) * 128;
-          const uint64_t bh = smem_desc(b_hi + boff, 128, b_sbo);
-          const uint64_t bl = smem_desc(b_lo + boff, 128, b_sbo);
+          const uint64_t ah = ah0 + (uint64_t)(g * 256 >> 4), al = ah + (uint64_t)(TR_OP_HALF >> 4);
+          const uint64_t bh = bh0 + (uint64_t)(g * 256 >> 4), bl = bh + (uint64_t)(b_half >> 4);
           mma_tf32(d, ah, bh, idesc, (c | g) ? 1u : 0u);
           mma_tf32(d, ah, bl, idesc, 1u);
           mma_tf32(d, al, bh, idesc, 1u);
@@ -272,6 +255,51 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a) {
       mma_commit(&done_bar);
       mbar_wait(&done_bar, 0);
     }
+  }
+  if (warp == TR_LOAD_WARP) {
+    // ---------------- loader ----------------
+    // one bulk copy (TMA engine) per row of a stage: 16 rows x up to 512 B, completing
+    // on the slot's raw_full barrier; rows beyond the inputs are not copied (the
+    // converters read zeros for them)
+    long long tile = blockIdx.x;
+    int c = 0;
+    long long issued = 0;
+    for (long long s = 0; s < nstages; ++s) {
+      const int slot = (int)(s & (TR_RAW - 1));
+      const uint32_t ur = (uint32_t)(s / TR_RAW);
+      if (abort_s) break;
+      bool ok = true;
+      if (lane == 0) ok = mbar_wait(&raw_empty[slot], (ur + 1) & 1);
+      if (!__shfl_sync(0xffffffffu, ok ? 1 : 0, 0)) {
+        if (lane == 0) {
+          abort_s = 1;
+          atomicExch(&g_tc_error, 1);
+        }
+        break;
+      }
+      const long long pos0 = tile * TR_M;
+      const long long left = a.n2 - pos0;
+      const uint32_t row_bytes = (uint32_t)(left >= TR_M ? TR_M * 4 : left * 4);
+      int nrows = a.m_tot - c * TR_JC;
+      nrows = nrows < 0 ? 0 : (nrows > TR_JC ? TR_JC : nrows);
+      if (lane == 0) mbar_arrive_expect_tx(&raw_full[slot], row_bytes * (uint32_t)nrows);
+      __syncwarp();
+      if (lane < nrows) {
+        const int j = c * TR_JC + lane;
+        const float* src = (j < a.m_in) ? a.S + (long long)j * a.n2 + pos0
+                                        : a.out + (long long)(j - a.m_in) * a.n2 + pos0;
+        bulk_copy_g2s(raw + slot * TR_RAW_BYTES + lane * (TR_M * 4), src, row_bytes, &raw_full[slot]);
+      }
+      issued = s + 1;
+      if (++c == a.nch) {
+        c = 0;
+        tile += gridDim.x;
+      }
+    }
+    // no copy may still be landing when the CTA exits: wait for the last issued phases
+    if (lane == 0)
+      for (long long s = issued - TR_RAW > 0 ? issued - TR_RAW : 0; s < issued; ++s)
+        mbar_wait(&raw_full[(int)(s & (TR_RAW - 1))], (uint32_t)((s / TR_RAW) & 1));
   }
   fence_before_sync();
   __syncthreads();
