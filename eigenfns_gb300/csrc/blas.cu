@@ -691,7 +691,7 @@ int noalloc_scratch(void** out) {
 }  // namespace
 
 namespace ef {
-int tc_rotate_max_rows(int m_out);
+int tc_rotate_max_rows(int m_out, int mode);
 int tc_rotate_launch(const float* C, int ldc, const float* S, float* out, int m_in, int m_out,
                      long long K, int mode, cudaStream_t st);
 }  // namespace ef
@@ -775,17 +775,17 @@ int ef_rotate(const float* C, const float* S, float* out, int m_in, int m_out, l
   const char* kern = getenv("EF_ROTATE_KERNEL");
   const bool simt = kern && strcmp(kern, "simt") == 0;
   if (!simt && tiled) {
-    // tensor cores: output groups of <= 64 columns; a pass holds `cap` input rows, the
-    // accumulate modes spend m_out of them on the current output
+    // tensor cores: output groups of <= 64 columns; a pass holds a bounded number of
+    // input rows (the accumulate modes also stage the current output)
     if (overlap) {
-      if (m_in + (mode != 0 ? m_out : 0) <= ef::tc_rotate_max_rows(m_out))
+      if (m_in <= ef::tc_rotate_max_rows(m_out, mode))
         return ef::tc_rotate_launch(C, m_out, S, out, m_in, m_out, K, mode, st);
     } else {
       int rc = EF_OK;
       for (int i0 = 0; i0 < m_out && rc == EF_OK; i0 += 64) {
         const int mo = m_out - i0 < 64 ? m_out - i0 : 64;
-        const int cap = ef::tc_rotate_max_rows(mo);
-        const int chunk = (mode == 0 && m_in <= cap) ? cap : cap - mo;
+        const int cap0 = ef::tc_rotate_max_rows(mo, mode);
+        const int chunk = m_in <= cap0 ? cap0 : ef::tc_rotate_max_rows(mo, 1);
         for (int j0 = 0; j0 < m_in && rc == EF_OK; j0 += chunk) {
           const int mi = m_in - j0 < chunk ? m_in - j0 : chunk;
           const int md = j0 == 0 ? mode : (mode == 0 ? 1 : mode);

@@ -15,16 +15,16 @@
 // registers while the next segment's MMAs run; a work unit's sum goes out in fp64
 // and units (K-chunks) are reduced in fp64.
 //
-// A persistent CTA (416 threads) walks work units (A-tile, B-tile, K-chunk):
-//   warps 0-7    converters: 16-byte cp.async of each stage's rows into a 4-deep
-//                shared raw ring (a converter-only named barrier per stage), hi/lo
-//                split (and the A' swap), 16-byte stores into a 3-deep ring of
-//                K-major operand stages;
+// A persistent CTA (448 threads) walks work units (A-tile, B-tile, K-chunk):
+//   warp 13      loads: one bulk copy (TMA engine) per row and stage into a 4-deep
+//                raw ring (mbarrier byte counts);
+//   warps 0-7    converters: hi/lo split (and the A' swap) of the raw stage, 16-byte
+//                stores into a 3-deep ring of K-major operand stages;
 //   warp 12      one thread issues each stage's MMAs and commits them;
 //   warps 8-11   drain finished segments (one TMEM lane per thread, all columns)
 //                and write the unit's partial sums.
 // Every mbarrier wait is bounded; on timeout the kernel sets the error flag, stops,
-// waits (bounded) for its own MMAs and frees its TMEM.
+// waits (bounded) for its own copies and MMAs and frees its TMEM.
 //
 // Reference: gram, eigenfns/solver.py:35-43 (true-fp32 X^H Y; the reference
 // forbids plain TF32, which floors the Gram at ~1e-3).
@@ -38,9 +38,10 @@ namespace {
 
 using namespace ef::tc;
 
-constexpr int GC_THREADS = 416;
+constexpr int GC_THREADS = 448;
 constexpr int GC_CONV = 256;          // converter threads (warps 0-7)
 constexpr int GC_MMA_WARP = 12;
+constexpr int GC_LOAD_WARP = 13;
 constexpr int GC_RAW_ROW = 144;       // raw ring row stride: 128 B of data + 16 B pad
 constexpr int GC_KB = 32;             // reals per stage (16 complex) = 4 k-steps of 8
 constexpr int GC_NBUF = 3;            // operand stages
@@ -68,7 +69,7 @@ struct GcArgs {
   int ma, mb, mt, nit, njt, nk;
 };
 
-// 13 warps: at most 4 per SM sub-partition, so 128 registers a thread fit
+// 14 warps: at most 4 per SM sub-partition, so 128 registers a thread fit
 template <int NB>
 __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a) {
   constexpr int B_BYTES = 2 * NB * GC_KB * 4;                  // [B_hi; B_lo]
@@ -78,6 +79,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t op_full[GC_NBUF], op_empty[GC_NBUF];
   __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done_bar;
+  __shared__ __align__(8) uint64_t raw_full[GC_RAW], raw_empty[GC_RAW];
   __shared__ uint32_t tmem_base_s;
   __shared__ volatile int abort_s;
 
@@ -99,6 +101,10 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a) {
       mbar_init(&acc_empty[b], 128);
     }
     mbar_init(&done_bar, 1);
+    for (int b = 0; b < GC_RAW; ++b) {
+      mbar_init(&raw_full[b], 1);
+      mbar_init(&raw_empty[b], GC_CONV);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   // operand rows the converters never write (A rows >= 2*mt) must read as zero
@@ -126,12 +132,10 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a) {
 
   if (warp < 8) {
     // ---------------- converters ----------------
-    // copy: the stage's rows (A rows [0, mt), B rows [mt, mt + NB)) as 16-byte chunks,
-    // 8 per row, into a shared raw ring whose rows are padded to 144 B; convert: item
-    // e -> row r = e % rows, quad q = e / rows, so consecutive threads take consecutive
-    // rows and both the raw reads and the 16-byte operand stores are conflict-free.
+    // item e -> row r = e % rows, quad q = e / rows: consecutive threads take consecutive
+    // rows, so the raw reads (rows padded to 144 B) and the 16-byte operand stores are
+    // conflict-free. Rows outside the matrices and quads past the unit's end read zero.
     const int rows = a.mt + NB;
-    // per-thread item geometry is stage-independent: computed once
     int cr[IPT], cq[IPT];
 #pragma unroll
     for (int u = 0; u < IPT; ++u) {
@@ -139,106 +143,68 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a) {
       cr[u] = e % rows;
       cq[u] = e / rows;
     }
-    long long s_issue = 0;
-    long long ku = 0;                                // issue cursor: unit, stage in unit
-    int it = 0, jt = 0, kc = 0, nst = 0, st_in = 0;
-    long long kbeg = 0;
-    if (my_units > 0) unit_of(0, it, jt, kc, kbeg, nst);
-    auto issue = [&]() {
-      while (ku < my_units && st_in >= nst) {
-        ++ku;
-        st_in = 0;
-        if (ku < my_units) unit_of(ku, it, jt, kc, kbeg, nst);
-      }
-      if (ku < my_units && !abort_s) {
-        const int i0 = it * a.mt, j0 = jt * NB;
-        const long long kc0 = kbeg + (long long)st_in * (GC_KB / 2);
-        long long kend = kbeg + a.kchunk;
-        if (kend > a.K) kend = a.K;
-        const uint32_t slot = smem_u32(raw + (int)(s_issue % GC_RAW) * RAW_BYTES);
+    long long s = 0;
+    for (long long k = 0; k < my_units && !abort_s; ++k) {
+      int it, jt, kc, nst;
+      long long kbeg;
+      unit_of(k, it, jt, kc, kbeg, nst);
+      long long kend = kbeg + a.kchunk;
+      if (kend > a.K) kend = a.K;
+      const int mrows = a.ma - it * a.mt, nrows = a.mb - jt * NB;
+      for (int st = 0; st < nst; ++st, ++s) {
+        const int slot = (int)(s % GC_RAW);
+        if (!mbar_wait(&raw_full[slot], (uint32_t)((s / GC_RAW) & 1))) {
+          abort_s = 1;
+          atomicExch(a.err, 1);
+          break;
+        }
+        const long long kc0 = kbeg + (long long)st * (GC_KB / 2);
+        const unsigned char* rs = raw + slot * RAW_BYTES;
+        float4 v[IPT];
 #pragma unroll
         for (int u = 0; u < IPT; ++u) {
-          const int ch = tid + u * GC_CONV;
-          const int r = ch >> 3, c = ch & 7;
-          const long long kq = kc0 + 2 * c;
-          bool in = r < rows && kq < kend;
-          const float* g = a.A;
-          if (in) {
+          const int e = tid + u * GC_CONV;
+          const int r = cr[u];
+          const bool rin = r < a.mt ? r < mrows : r - a.mt < nrows;
+          v[u] = (e < nitems && rin && kc0 + 2 * cq[u] < kend)
+                     ? *reinterpret_cast<const float4*>(rs + r * GC_RAW_ROW + cq[u] * 16)
+                     : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        mbar_arrive(&raw_empty[slot]);
+        const int o = (int)(s % GC_NBUF);
+        if (!mbar_wait(&op_empty[o], (uint32_t)(((s / GC_NBUF) + 1) & 1))) {
+          abort_s = 1;
+          atomicExch(a.err, 1);
+          break;
+        }
+        unsigned char* base = smem + o * OP_BYTES;
+#pragma unroll
+        for (int u = 0; u < IPT; ++u) {
+          const int e = tid + u * GC_CONV;
+          if (e < nitems) {
+            const int r = cr[u], q = cq[u];
+            const float4 x = v[u];
+            const float4 h = make_float4(tf32_rn(x.x), tf32_rn(x.y), tf32_rn(x.z), tf32_rn(x.w));
+            const float4 l = make_float4(tf32_rn(x.x - h.x), tf32_rn(x.y - h.y), tf32_rn(x.z - h.z),
+                                         tf32_rn(x.w - h.w));
             if (r < a.mt) {
-              in = i0 + r < a.ma;
-              g = a.A + ((long long)(i0 + r) * a.K + kq) * 2;
+              *reinterpret_cast<float4*>(base + quad_off(r, q)) = h;
+              *reinterpret_cast<float4*>(base + GC_A_HALF + quad_off(r, q)) = l;
+              // A' = (-ai, ar) per complex: swap within the pairs and negate the new real part
+              *reinterpret_cast<float4*>(base + quad_off(a.mt + r, q)) = make_float4(-h.y, h.x, -h.w, h.z);
+              *reinterpret_cast<float4*>(base + GC_A_HALF + quad_off(a.mt + r, q)) =
+                  make_float4(-l.y, l.x, -l.w, l.z);
             } else {
-              in = j0 + r - a.mt < a.mb;
-              g = a.B + ((long long)(j0 + r - a.mt) * a.K + kq) * 2;
+              const int rb = r - a.mt;
+              *reinterpret_cast<float4*>(base + 2 * GC_A_HALF + quad_off(rb, q)) = h;
+              *reinterpret_cast<float4*>(base + 2 * GC_A_HALF + quad_off(NB + rb, q)) = l;
             }
           }
-          if (r < rows)
-            asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(slot + r * GC_RAW_ROW + c * 16),
-                         "l"(in ? g : a.A), "r"(in ? 16 : 0) : "memory");
         }
+        fence_async_smem();
+        mbar_arrive(&op_full[o]);
       }
-      if (ku < my_units) {
-        ++st_in;
-        ++s_issue;
-      }
-      asm volatile("cp.async.commit_group;" ::: "memory");
-    };
-    long long total = 0;
-    for (long long k = 0; k < my_units; ++k) {
-      int i1, j1, k1, n1;
-      long long b1;
-      unit_of(k, i1, j1, k1, b1, n1);
-      total += n1;
     }
-    for (int s = 0; s < GC_RAW - 1; ++s) issue();
-    // every converter thread runs every iteration (named barrier counts stay uniform)
-    for (long long s = 0; s < total; ++s) {
-      asm volatile("cp.async.wait_group %0;" ::"n"(GC_RAW - 2) : "memory");
-      asm volatile("bar.sync 1, %0;" ::"n"(GC_CONV) : "memory");
-      issue();                                      // refills the slot all threads finished reading
-      const unsigned char* rs = raw + (int)(s % GC_RAW) * RAW_BYTES;
-      float4 v[IPT];
-#pragma unroll
-      for (int u = 0; u < IPT; ++u) {
-        const int e = tid + u * GC_CONV;
-        v[u] = e < nitems ? *reinterpret_cast<const float4*>(rs + cr[u] * GC_RAW_ROW + cq[u] * 16)
-                          : make_float4(0.f, 0.f, 0.f, 0.f);
-      }
-      const int o = (int)(s % GC_NBUF);
-      if (abort_s) continue;
-      if (!mbar_wait(&op_empty[o], (uint32_t)(((s / GC_NBUF) + 1) & 1))) {
-        abort_s = 1;
-        atomicExch(a.err, 1);
-        continue;
-      }
-      unsigned char* base = smem + o * OP_BYTES;
-#pragma unroll
-      for (int u = 0; u < IPT; ++u) {
-        const int e = tid + u * GC_CONV;
-        if (e < nitems) {
-          const int r = cr[u], q = cq[u];
-          const float4 x = v[u];
-          const float4 h = make_float4(tf32_rn(x.x), tf32_rn(x.y), tf32_rn(x.z), tf32_rn(x.w));
-          const float4 l = make_float4(tf32_rn(x.x - h.x), tf32_rn(x.y - h.y), tf32_rn(x.z - h.z),
-                                       tf32_rn(x.w - h.w));
-          if (r < a.mt) {
-            *reinterpret_cast<float4*>(base + quad_off(r, q)) = h;
-            *reinterpret_cast<float4*>(base + GC_A_HALF + quad_off(r, q)) = l;
-            // A' = (-ai, ar) per complex: swap within the pairs and negate the new real part
-            *reinterpret_cast<float4*>(base + quad_off(a.mt + r, q)) = make_float4(-h.y, h.x, -h.w, h.z);
-            *reinterpret_cast<float4*>(base + GC_A_HALF + quad_off(a.mt + r, q)) =
-                make_float4(-l.y, l.x, -l.w, l.z);
-          } else {
-            const int rb = r - a.mt;
-            *reinterpret_cast<float4*>(base + 2 * GC_A_HALF + quad_off(rb, q)) = h;
-            *reinterpret_cast<float4*>(base + 2 * GC_A_HALF + quad_off(NB + rb, q)) = l;
-          }
-        }
-      }
-      fence_async_smem();
-      mbar_arrive(&op_full[o]);
-    }
-    asm volatile("cp.async.wait_group 0;" ::: "memory");
   } else if (warp < 12) {
     // ---------------- drain ----------------
     const int lq = warp & 3;
@@ -335,6 +301,53 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a) {
       mma_commit(&done_bar);
       mbar_wait(&done_bar, 0);
     }
+  }
+  if (warp == GC_LOAD_WARP) {
+    // ---------------- loader ----------------
+    // one bulk copy (TMA engine) per row and stage: 16 complex = 128 B of every valid
+    // A and B row into the raw ring (rows 144 B apart), counted on raw_full in bytes
+    long long s = 0, issued = 0;
+    for (long long k = 0; k < my_units && !abort_s; ++k) {
+      int it, jt, kc, nst;
+      long long kbeg;
+      unit_of(k, it, jt, kc, kbeg, nst);
+      long long kend = kbeg + a.kchunk;
+      if (kend > a.K) kend = a.K;
+      const int i0 = it * a.mt, j0 = jt * NB;
+      const int mrows = a.ma - i0 < a.mt ? a.ma - i0 : a.mt;
+      const int nrows = a.mb - j0 < NB ? a.mb - j0 : NB;
+      for (int st = 0; st < nst; ++st, ++s) {
+        const int slot = (int)(s % GC_RAW);
+        bool ok = true;
+        if (lane == 0) ok = mbar_wait(&raw_empty[slot], (uint32_t)(((s / GC_RAW) + 1) & 1));
+        if (!__shfl_sync(0xffffffffu, ok ? 1 : 0, 0)) {
+          if (lane == 0) {
+            abort_s = 1;
+            atomicExch(a.err, 1);
+          }
+          break;
+        }
+        const long long kc0 = kbeg + (long long)st * (GC_KB / 2);
+        const long long left = kend - kc0;
+        const uint32_t bytes = (uint32_t)((left >= GC_KB / 2 ? GC_KB / 2 : left) * 8);
+        if (lane == 0) mbar_arrive_expect_tx(&raw_full[slot], bytes * (uint32_t)(mrows + nrows));
+        __syncwarp();
+        unsigned char* dst = raw + slot * RAW_BYTES;
+        for (int r = lane; r < a.mt + NB; r += 32) {
+          const bool isa = r < a.mt;
+          if (isa ? r < mrows : r - a.mt < nrows) {
+            const float* src = isa ? a.A + ((long long)(i0 + r) * a.K + kc0) * 2
+                                   : a.B + ((long long)(j0 + r - a.mt) * a.K + kc0) * 2;
+            bulk_copy_g2s(dst + r * GC_RAW_ROW, src, bytes, &raw_full[slot]);
+          }
+        }
+        issued = s + 1;
+      }
+    }
+    // no copy may still be landing when the CTA exits: wait for the last issued phases
+    if (lane == 0)
+      for (long long t = issued - GC_RAW > 0 ? issued - GC_RAW : 0; t < issued; ++t)
+        mbar_wait(&raw_full[(int)(t % GC_RAW)], (uint32_t)((t / GC_RAW) & 1));
   }
   fence_before_sync();
   __syncthreads();

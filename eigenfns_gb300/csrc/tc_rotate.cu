@@ -8,26 +8,30 @@
 // gives the complex result. Three TF32 products per pair (x = hi + lo) give
 // fp32-class accuracy: D += A_hi B_hi + A_hi B_lo + A_lo B_hi.
 // The accumulate modes out (+/-)= ... fold the current output into the same GEMM:
-// its m_out rows are appended to S with identity coefficients and C is negated for
-// subtraction, so every mode ends in a plain store.
+// its m_out rows are appended to S (from the next 16-row boundary) with identity
+// coefficients and C is negated for subtraction, so every mode ends in a plain store.
 //
 // Tiles are 128 real positions (M = 128 TMEM lanes); N = 2 * m_out padded to 8.
 // A persistent CTA (448 threads) walks its tiles with four warp roles:
-//   warp 13     loads: one bulk copy (TMA engine) per 512-byte row of a 16-row x
-//               128-position stage into an 8-deep raw ring (mbarrier byte counts);
-//   warps 0-7   convert: read the raw stage (one position per thread), split hi/lo,
-//               store 16-byte quads into a 3-deep ring of K-major operand stages;
-//   warp 12     one thread issues the MMAs of each stage into one of two TMEM
+//   warp 13     loads: one 2-D TMA box (16 rows x 128 positions, 8 KB, zero fill
+//               outside the matrix) per stage into a raw shared-memory ring;
+//   warps 0-7   convert: each thread owns one position (= one TMEM lane) and 8 rows
+//               of the stage, splits hi/lo and writes them with tcgen05.st into a
+//               ring of TMEM operand stages (the MMA's A operand lives in TMEM);
+//   warp 12     one thread issues the MMAs of each stage (A from TMEM, the resident
+//               coefficient operand B from shared memory) into one of two TMEM
 //               accumulators and commits them to the stage's "empty" barrier;
 //   warps 8-11  drain a finished accumulator (tcgen05.ld, one lane per thread),
 //               combine D1/D2 with a lane exchange and store.
-// The coefficient operand [Re C | Im C] (hi and lo) is built once per CTA and stays
-// resident in shared memory. Every mbarrier wait is bounded: on timeout the kernel
-// sets the library's device error flag and stops issuing work, waits (bounded) for
-// its own copies and MMAs and frees its TMEM.
+// Every mbarrier wait is bounded: on timeout the kernel sets the library's device
+// error flag and stops issuing work, waits (bounded) for its own copies and MMAs and
+// frees its TMEM.
 //
 // Reference: tensordot(C.T, S) in combine / rotations, eigenfns/solver.py:49-57,106,125.
+#include <cuda.h>
+
 #include <cstdint>
+#include <mutex>
 
 #include "common.cuh"
 #include "status.h"
@@ -44,27 +48,26 @@ constexpr int TR_MMA_WARP = 12;
 constexpr int TR_LOAD_WARP = 13;
 constexpr int TR_M = 128;                 // real positions per tile
 constexpr int TR_JC = 16;                 // rows of S per stage
-constexpr int TR_NBUF = 3;                // operand stages in the ring
-constexpr int TR_OP_HALF = TR_M * TR_JC * 4;       // 8 KB: hi or lo of one stage
-constexpr int TR_OP_BYTES = 2 * TR_OP_HALF;        // 16 KB per stage
-constexpr int TR_RAW = 8;                 // raw stages in flight (power of two)
-constexpr int TR_RAW_BYTES = TR_JC * TR_M * 4;     // 8 KB per raw stage (row-major)
+constexpr int TR_NBUF = 4;                // TMEM operand stages (hi + lo: 2*TR_JC columns each)
+constexpr int TR_RAW = 12;                // raw shared-memory stages
+constexpr int TR_RAW_BYTES = TR_JC * TR_M * 4;     // 8 KB per raw stage (row-major box)
 constexpr int TR_SMEM_MAX = 227 * 1024 - 1024;   // dynamic part; static barriers take the rest
+constexpr int TR_SMEM_MIN = 120 * 1024;          // keeps one CTA (and its TMEM) per SM
 
 __device__ int g_tc_error = 0;
 
 struct TrArgs {
   const float2* C;      // (m_in, ldc) complex, columns [0, m_out) used
-  const float* S;       // m_in rows of n2 floats
-  float* out;           // m_out rows of n2 floats (also the identity rows when mode != 0)
+  float* out;           // m_out rows of n2 floats
   long long n2;         // 2K
   long long ntiles;
-  int ldc, m_in, m_tot, m_out, mp, nch;
+  int ldc, m_in, m_out, mp, ncs, nch;
   float sign;           // -1 for subtraction
 };
 
 // 14 warps: at most 4 per SM sub-partition, so 128 registers a thread fit
-__global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a) {
+__global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_constant__ CUtensorMap map_s,
+                                                  const __grid_constant__ CUtensorMap map_o) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t op_full[TR_NBUF], op_empty[TR_NBUF];
   __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done_bar;
@@ -74,11 +77,12 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a) {
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int N = 2 * a.mp;
-  const int kj = a.nch * TR_JC;            // padded rows of the coefficient operand
+  const int kj = a.nch * TR_JC;            // rows of the coefficient operand
   const uint32_t b_half = (uint32_t)N * kj * 4;
-  unsigned char* raw = smem + TR_NBUF * TR_OP_BYTES;
+  unsigned char* raw = smem;
   unsigned char* bops = raw + TR_RAW * TR_RAW_BYTES;
-  const uint32_t tcols = tmem_cols_for(2 * N);
+  const uint32_t col_a = (uint32_t)(2 * N);                // first TMEM operand column
+  const uint32_t tcols = tmem_cols_for(2 * N + TR_NBUF * 2 * TR_JC);
 
   if (tid == 0) {
     abort_s = 0;
@@ -97,9 +101,9 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a) {
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // coefficient operand, K-major core matrices: row n (D column), column j (row of S)
-  // rows [0, mp) = Re C[:, n], rows [mp, 2mp) = Im C[:, n - mp]; rows j >= m_in of
-  // the inputs are the current output (identity coefficients); zero padding elsewhere
+  // coefficient operand, K-major core matrices: row n (D column), column j (input row)
+  // rows [0, mp) = Re C[:, n], rows [mp, 2mp) = Im C[:, n - mp]. Inputs j < 16*ncs are
+  // S rows (coefficient 0 past m_in), inputs 16*ncs + i are output rows i (identity).
   for (int e = tid; e < (int)(2 * b_half / 16); e += TR_THREADS)
     reinterpret_cast<float4*>(bops)[e] = make_float4(0.f, 0.f, 0.f, 0.f);
   __syncthreads();
@@ -116,7 +120,8 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a) {
     put(i, j, a.sign * c.x);
     put(a.mp + i, j, a.sign * c.y);
   }
-  for (int i = tid; i < a.m_tot - a.m_in; i += TR_THREADS) put(i, a.m_in + i, 1.f);
+  if (a.nch > a.ncs)
+    for (int i = tid; i < a.m_out; i += TR_THREADS) put(i, a.ncs * TR_JC + i, 1.f);
   fence_async_smem();
   if (warp == TR_MMA_WARP) tmem_alloc(&tmem_base_s, tcols);
   fence_before_sync();
@@ -129,50 +134,40 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a) {
 
   if (warp < 8) {
     // ---------------- converters ----------------
-    // each thread owns position p and rows 8h..8h+7 of a stage (conflict-free reads)
-    const int p = tid & (TR_M - 1), h = tid >> 7;
-    long long cur_tile = blockIdx.x;
-    int cur_c = 0;
+    // warp w writes TMEM lane quarter w % 4; thread = position p = lane of its quarter;
+    // warps 0-3 take rows 0-7 of a stage, warps 4-7 rows 8-15
+    const int q4 = warp & 3, hv = warp >> 2;
+    const int p = q4 * 32 + lane;
+    const uint32_t lane_base = tmem + ((uint32_t)(q4 * 32) << 16);
     for (long long s = 0; s < nstages; ++s) {
-      const int slot = (int)(s & (TR_RAW - 1));
-      const uint32_t ur = (uint32_t)(s / TR_RAW);
+      const int slot = (int)(s % TR_RAW);
       if (abort_s) break;
-      if (!mbar_wait(&raw_full[slot], ur & 1)) {
+      if (!mbar_wait(&raw_full[slot], (uint32_t)((s / TR_RAW) & 1))) {
         abort_s = 1;
         atomicExch(&g_tc_error, 1);
         break;
       }
       const float* rs = reinterpret_cast<const float*>(raw + slot * TR_RAW_BYTES) + p;
-      const bool pin = cur_tile * TR_M + p < a.n2;
-      const int j0 = cur_c * TR_JC + h * 8;
-      float v[8];
+      float hi[8], lo[8];
 #pragma unroll
-      for (int r = 0; r < 8; ++r) v[r] = (pin && j0 + r < a.m_tot) ? rs[(h * 8 + r) * TR_M] : 0.f;
-      mbar_arrive(&raw_empty[slot]);
-      if (++cur_c == a.nch) {
-        cur_c = 0;
-        cur_tile += gridDim.x;
+      for (int r = 0; r < 8; ++r) {
+        const float x = rs[(hv * 8 + r) * TR_M];
+        hi[r] = tf32_rn(x);
+        lo[r] = tf32_rn(x - hi[r]);
       }
+      mbar_arrive(&raw_empty[slot]);
       const int o = (int)(s % TR_NBUF);
-      const uint32_t u = (uint32_t)(s / TR_NBUF);
-      if (!mbar_wait(&op_empty[o], (u + 1) & 1)) {
+      if (!mbar_wait(&op_empty[o], (uint32_t)(((s / TR_NBUF) + 1) & 1))) {
         abort_s = 1;
         atomicExch(&g_tc_error, 1);
         break;
       }
-      unsigned char* base = smem + o * TR_OP_BYTES;
-#pragma unroll
-      for (int qq = 0; qq < 2; ++qq) {
-        const int q = h * 2 + qq;
-        const float4 x = make_float4(v[4 * qq], v[4 * qq + 1], v[4 * qq + 2], v[4 * qq + 3]);
-        const float4 hi = make_float4(tf32_rn(x.x), tf32_rn(x.y), tf32_rn(x.z), tf32_rn(x.w));
-        const float4 lo = make_float4(tf32_rn(x.x - hi.x), tf32_rn(x.y - hi.y), tf32_rn(x.z - hi.z),
-                                      tf32_rn(x.w - hi.w));
-        const int off = (((p >> 3) * (TR_JC / 4) + q) << 7) + ((p & 7) << 4);
-        *reinterpret_cast<float4*>(base + off) = hi;
-        *reinterpret_cast<float4*>(base + TR_OP_HALF + off) = lo;
-      }
-      fence_async_smem();
+      fence_after_sync();
+      const uint32_t col = col_a + (uint32_t)(o * 2 * TR_JC + hv * 8);
+      tmem_st8(lane_base + col, hi);
+      tmem_st8(lane_base + col + TR_JC, lo);
+      tmem_wait_st();
+      fence_before_sync();
       mbar_arrive(&op_full[o]);
     }
   } else if (warp < 12) {
@@ -209,10 +204,7 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a) {
   } else if (warp == TR_MMA_WARP && lane == 0) {
     // ---------------- MMA issue ----------------
     const uint32_t idesc = idesc_tf32(TR_M, N);
-    const uint32_t b_hi = smem_u32(bops);
-    const uint32_t b_sbo = (uint32_t)kq * 128;
-    const uint64_t a_desc0 = smem_desc(smem_u32(smem), 128, (TR_JC / 4) * 128);
-    const uint64_t b_desc0 = smem_desc(b_hi, 128, b_sbo);
+    const uint64_t b_desc0 = smem_desc(smem_u32(bops), 128, (uint32_t)kq * 128);
     bool issued = false;
     for (long long k = 0; k < my_tiles && !abort_s; ++k) {
       const int ab = (int)(k & 1);
@@ -232,17 +224,15 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a) {
           break;
         }
         fence_after_sync();
-        // descriptors differ from the base ones only in the start-address field
-        const uint64_t ah0 = a_desc0 + (uint64_t)((o * TR_OP_BYTES) >> 4);
+        const uint32_t a_hi = tmem + col_a + (uint32_t)(o * 2 * TR_JC), a_lo = a_hi + TR_JC;
+        // descriptors differ from the base one only in the start-address field
         const uint64_t bh0 = b_desc0 + (uint64_t)((c * (TR_JC / 4) * 128) >> 4);
 #pragma unroll
         for (int g = 0; g < TR_JC / 8; ++g) {
-          if (c * TR_JC + g * 8 >= a.m_tot) break;      // all-zero rows: nothing to add
-          const uint64_t ah = ah0 + (uint64_t)(g * 256 >> 4), al = ah + (uint64_t)(TR_OP_HALF >> 4);
           const uint64_t bh = bh0 + (uint64_t)(g * 256 >> 4), bl = bh + (uint64_t)(b_half >> 4);
-          mma_tf32(d, ah, bh, idesc, (c | g) ? 1u : 0u);
-          mma_tf32(d, ah, bl, idesc, 1u);
-          mma_tf32(d, al, bh, idesc, 1u);
+          mma_tf32_ts(d, a_hi + 8 * g, bh, idesc, (c | g) ? 1u : 0u);
+          mma_tf32_ts(d, a_hi + 8 * g, bl, idesc, 1u);
+          mma_tf32_ts(d, a_lo + 8 * g, bh, idesc, 1u);
         }
         mma_commit(&op_empty[o]);
         issued = true;
@@ -255,41 +245,26 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a) {
       mma_commit(&done_bar);
       mbar_wait(&done_bar, 0);
     }
-  }
-  if (warp == TR_LOAD_WARP) {
+  } else if (warp == TR_LOAD_WARP && lane == 0) {
     // ---------------- loader ----------------
-    // one bulk copy (TMA engine) per row of a stage: 16 rows x up to 512 B, completing
-    // on the slot's raw_full barrier; rows beyond the inputs are not copied (the
-    // converters read zeros for them)
+    // one 2-D TMA box per stage: rows [16c, 16c + 16) of S (chunks c < ncs) or of the
+    // output (chunks c >= ncs), positions [128 t, 128 t + 128); outside the matrix the
+    // box reads zeros. The transaction count is the full box.
     long long tile = blockIdx.x;
     int c = 0;
     long long issued = 0;
     for (long long s = 0; s < nstages; ++s) {
-      const int slot = (int)(s & (TR_RAW - 1));
-      const uint32_t ur = (uint32_t)(s / TR_RAW);
+      const int slot = (int)(s % TR_RAW);
       if (abort_s) break;
-      bool ok = true;
-      if (lane == 0) ok = mbar_wait(&raw_empty[slot], (ur + 1) & 1);
-      if (!__shfl_sync(0xffffffffu, ok ? 1 : 0, 0)) {
-        if (lane == 0) {
-          abort_s = 1;
-          atomicExch(&g_tc_error, 1);
-        }
+      if (!mbar_wait(&raw_empty[slot], (uint32_t)(((s / TR_RAW) + 1) & 1))) {
+        abort_s = 1;
+        atomicExch(&g_tc_error, 1);
         break;
       }
-      const long long pos0 = tile * TR_M;
-      const long long left = a.n2 - pos0;
-      const uint32_t row_bytes = (uint32_t)(left >= TR_M ? TR_M * 4 : left * 4);
-      int nrows = a.m_tot - c * TR_JC;
-      nrows = nrows < 0 ? 0 : (nrows > TR_JC ? TR_JC : nrows);
-      if (lane == 0) mbar_arrive_expect_tx(&raw_full[slot], row_bytes * (uint32_t)nrows);
-      __syncwarp();
-      if (lane < nrows) {
-        const int j = c * TR_JC + lane;
-        const float* src = (j < a.m_in) ? a.S + (long long)j * a.n2 + pos0
-                                        : a.out + (long long)(j - a.m_in) * a.n2 + pos0;
-        bulk_copy_g2s(raw + slot * TR_RAW_BYTES + lane * (TR_M * 4), src, row_bytes, &raw_full[slot]);
-      }
+      mbar_arrive_expect_tx(&raw_full[slot], TR_RAW_BYTES);
+      const int x = (int)(tile * TR_M);
+      if (c < a.ncs) tma_load_2d(raw + slot * TR_RAW_BYTES, &map_s, x, c * TR_JC, &raw_full[slot]);
+      else tma_load_2d(raw + slot * TR_RAW_BYTES, &map_o, x, (c - a.ncs) * TR_JC, &raw_full[slot]);
       issued = s + 1;
       if (++c == a.nch) {
         c = 0;
@@ -297,9 +272,8 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a) {
       }
     }
     // no copy may still be landing when the CTA exits: wait for the last issued phases
-    if (lane == 0)
-      for (long long s = issued - TR_RAW > 0 ? issued - TR_RAW : 0; s < issued; ++s)
-        mbar_wait(&raw_full[(int)(s & (TR_RAW - 1))], (uint32_t)((s / TR_RAW) & 1));
+    for (long long s = issued - TR_RAW > 0 ? issued - TR_RAW : 0; s < issued; ++s)
+      mbar_wait(&raw_full[(int)(s % TR_RAW)], (uint32_t)((s / TR_RAW) & 1));
   }
   fence_before_sync();
   __syncthreads();
@@ -320,49 +294,85 @@ int sm_count() {
   return cached[dev];
 }
 
-size_t tr_smem(int m_tot, int mp) {
-  const int nch = (m_tot + TR_JC - 1) / TR_JC;
-  return (size_t)TR_NBUF * TR_OP_BYTES + (size_t)TR_RAW * TR_RAW_BYTES +
-         (size_t)2 * (2 * mp) * (nch * TR_JC) * 4;
+size_t tr_smem(int nch, int mp) {
+  const size_t s = (size_t)TR_RAW * TR_RAW_BYTES + (size_t)2 * (2 * mp) * (nch * TR_JC) * 4;
+  return s < (size_t)TR_SMEM_MIN ? (size_t)TR_SMEM_MIN : s;
+}
+
+int chunks_for(int m_in, int m_out, int mode) {
+  return (m_in + TR_JC - 1) / TR_JC + (mode != 0 ? (m_out + TR_JC - 1) / TR_JC : 0);
+}
+
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_fn() {
+  static EncodeTiled fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiled>(p);
+  });
+  return fn;
+}
+
+// rows x n2 fp32 matrix, boxes of 16 rows x 128 floats, zero fill outside
+bool make_map(CUtensorMap* m, const float* base, int rows, long long n2) {
+  EncodeTiled fn = encode_fn();
+  if (!fn) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)n2, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)n2 * 4};
+  const cuuint32_t box[2] = {TR_M, TR_JC};
+  const cuuint32_t estr[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 }  // namespace
 
 namespace ef {
 
-// largest number of input rows (S rows plus, in the accumulate modes, the m_out
-// output rows) one tensor-core pass holds for m_out outputs; 0 when m_out > 64
-int tc_rotate_max_rows(int m_out) {
+// largest number of S rows one tensor-core pass holds for m_out outputs in `mode`
+// (the accumulate modes also stage the m_out output rows); 0 when m_out > 64
+int tc_rotate_max_rows(int m_out, int mode) {
   if (m_out <= 0 || m_out > 64) return 0;
   const int mp = (m_out + 7) / 8 * 8;
   int rows = 0;
-  while (tr_smem(rows + TR_JC, mp) <= (size_t)TR_SMEM_MAX) rows += TR_JC;
+  while (tr_smem(chunks_for(rows + TR_JC, m_out, mode), mp) <= (size_t)TR_SMEM_MAX) rows += TR_JC;
   return rows;
 }
 
-// one pass: m_out <= 64, m_in + (mode ? m_out : 0) <= tc_rotate_max_rows(m_out);
-// S and out 16-byte aligned, K even
+// one pass: m_out <= 64, m_in <= tc_rotate_max_rows(m_out, mode); S and out 16-byte
+// aligned, K even
 int tc_rotate_launch(const float* C, int ldc, const float* S, float* out, int m_in, int m_out,
                      long long K, int mode, cudaStream_t st) {
   TrArgs a;
   a.C = (const float2*)C;
-  a.S = S;
   a.out = out;
   a.n2 = 2 * K;
   a.ntiles = (a.n2 + TR_M - 1) / TR_M;
   a.ldc = ldc;
   a.m_in = m_in;
   a.m_out = m_out;
-  a.m_tot = m_in + (mode != 0 ? m_out : 0);
   a.mp = (m_out + 7) / 8 * 8;
-  a.nch = (a.m_tot + TR_JC - 1) / TR_JC;
+  a.ncs = (m_in + TR_JC - 1) / TR_JC;
+  a.nch = chunks_for(m_in, m_out, mode);
   a.sign = mode < 0 ? -1.f : 1.f;
-  const size_t smem = tr_smem(a.m_tot, a.mp);
+  CUtensorMap ms, mo;
+  if (!make_map(&ms, S, m_in, a.n2) || !make_map(&mo, out, m_out, a.n2))
+    return ef_fail(EF_ERR_CUDA, "rotate: tensor map encoding failed");
+  const size_t smem = tr_smem(a.nch, a.mp);
   ef::set_smem_once(tc_rotate_kernel, smem);
   long long grid = sm_count();
   if (grid > a.ntiles) grid = a.ntiles;
   ef_count_launches(1);
-  tc_rotate_kernel<<<(unsigned)grid, TR_THREADS, smem, st>>>(a);
+  tc_rotate_kernel<<<(unsigned)grid, TR_THREADS, smem, st>>>(a, ms, mo);
   return ef_check_launch();
 }
 
