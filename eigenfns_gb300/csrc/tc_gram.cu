@@ -28,11 +28,14 @@
 //
 // Reference: gram, eigenfns/solver.py:35-43 (true-fp32 X^H Y; the reference
 // forbids plain TF32, which floors the Gram at ~1e-3).
+#include <cuda.h>
+
 #include <cstdint>
 
 #include "common.cuh"
 #include "status.h"
 #include "tc_common.cuh"
+#include "tmap.h"
 
 namespace {
 
@@ -42,7 +45,6 @@ constexpr int GC_THREADS = 448;
 constexpr int GC_CONV = 256;          // converter threads (warps 0-7)
 constexpr int GC_MMA_WARP = 12;
 constexpr int GC_LOAD_WARP = 13;
-constexpr int GC_RAW_ROW = 144;       // raw ring row stride: 128 B of data + 16 B pad
 constexpr int GC_KB = 32;             // reals per stage (16 complex) = 4 k-steps of 8
 constexpr int GC_NBUF = 3;            // operand stages
 constexpr int GC_RAW = 4;             // raw stages per converter thread
@@ -71,11 +73,12 @@ struct GcArgs {
 
 // 14 warps: at most 4 per SM sub-partition, so 128 registers a thread fit
 template <int NB>
-__global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a) {
+__global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_constant__ CUtensorMap map_a,
+                                                const __grid_constant__ CUtensorMap map_b) {
   constexpr int B_BYTES = 2 * NB * GC_KB * 4;                  // [B_hi; B_lo]
   constexpr int OP_BYTES = 2 * GC_A_HALF + B_BYTES;
   constexpr int IPT = ((64 + NB) * (GC_KB / 4) + GC_CONV - 1) / GC_CONV;   // items per thread
-  constexpr int RAW_BYTES = (64 + NB) * GC_RAW_ROW;
+  constexpr int RAW_BYTES = (64 + NB) * 128;                   // A box + B box, 128-B rows
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t op_full[GC_NBUF], op_empty[GC_NBUF];
   __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done_bar;
@@ -84,7 +87,9 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a) {
   __shared__ volatile int abort_s;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  unsigned char* raw = smem + GC_NBUF * OP_BYTES;
+  // raw boxes use the 128-byte swizzle, which wants 1024-byte aligned stages
+  unsigned char* raw = smem + ((1024u - (smem_u32(smem) & 1023u)) & 1023u);
+  unsigned char* ops = raw + GC_RAW * RAW_BYTES;
   constexpr uint32_t TCOLS = tmem_cols_for(4 * NB);
   const int nitems = (a.mt + NB) * (GC_KB / 4);                // items per stage
   const long long units = (long long)a.nit * a.njt * a.nk;
@@ -109,7 +114,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a) {
   }
   // operand rows the converters never write (A rows >= 2*mt) must read as zero
   for (int e = tid; e < GC_NBUF * OP_BYTES / 16; e += GC_THREADS)
-    reinterpret_cast<float4*>(smem)[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+    reinterpret_cast<float4*>(ops)[e] = make_float4(0.f, 0.f, 0.f, 0.f);
   fence_async_smem();
   if (warp == GC_MMA_WARP) tmem_alloc(&tmem_base_s, TCOLS);
   fence_before_sync();
@@ -167,7 +172,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a) {
           const int r = cr[u];
           const bool rin = r < a.mt ? r < mrows : r - a.mt < nrows;
           v[u] = (e < nitems && rin && kc0 + 2 * cq[u] < kend)
-                     ? *reinterpret_cast<const float4*>(rs + r * GC_RAW_ROW + cq[u] * 16)
+                     ? *reinterpret_cast<const float4*>(rs + r * 128 + ((cq[u] ^ (r & 7)) << 4))
                      : make_float4(0.f, 0.f, 0.f, 0.f);
         }
         mbar_arrive(&raw_empty[slot]);
@@ -177,7 +182,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a) {
           atomicExch(a.err, 1);
           break;
         }
-        unsigned char* base = smem + o * OP_BYTES;
+        unsigned char* base = ops + o * OP_BYTES;
 #pragma unroll
         for (int u = 0; u < IPT; ++u) {
           const int e = tid + u * GC_CONV;
@@ -256,7 +261,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a) {
   } else if (warp == GC_MMA_WARP && lane == 0) {
     // ---------------- MMA issue ----------------
     const uint32_t id1 = idesc_tf32(128, 2 * NB), id2 = idesc_tf32(128, NB);
-    const uint64_t desc0 = gram_desc(smem_u32(smem));
+    const uint64_t desc0 = gram_desc(smem_u32(ops));
     long long s = 0, q = 0;
     bool issued = false;
     for (long long k = 0; k < my_units && !abort_s; ++k) {
@@ -304,18 +309,14 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a) {
   }
   if (warp == GC_LOAD_WARP) {
     // ---------------- loader ----------------
-    // one bulk copy (TMA engine) per row and stage: 16 complex = 128 B of every valid
-    // A and B row into the raw ring (rows 144 B apart), counted on raw_full in bytes
+    // per stage one 2-D box of the unit's A rows and one of its B rows (16 complex =
+    // 128 B per row), counted on raw_full in bytes
     long long s = 0, issued = 0;
     for (long long k = 0; k < my_units && !abort_s; ++k) {
       int it, jt, kc, nst;
       long long kbeg;
       unit_of(k, it, jt, kc, kbeg, nst);
-      long long kend = kbeg + a.kchunk;
-      if (kend > a.K) kend = a.K;
       const int i0 = it * a.mt, j0 = jt * NB;
-      const int mrows = a.ma - i0 < a.mt ? a.ma - i0 : a.mt;
-      const int nrows = a.mb - j0 < NB ? a.mb - j0 : NB;
       for (int st = 0; st < nst; ++st, ++s) {
         const int slot = (int)(s % GC_RAW);
         bool ok = true;
@@ -328,19 +329,14 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a) {
           break;
         }
         const long long kc0 = kbeg + (long long)st * (GC_KB / 2);
-        const long long left = kend - kc0;
-        const uint32_t bytes = (uint32_t)((left >= GC_KB / 2 ? GC_KB / 2 : left) * 8);
-        if (lane == 0) mbar_arrive_expect_tx(&raw_full[slot], bytes * (uint32_t)(mrows + nrows));
-        __syncwarp();
-        unsigned char* dst = raw + slot * RAW_BYTES;
-        for (int r = lane; r < a.mt + NB; r += 32) {
-          const bool isa = r < a.mt;
-          if (isa ? r < mrows : r - a.mt < nrows) {
-            const float* src = isa ? a.A + ((long long)(i0 + r) * a.K + kc0) * 2
-                                   : a.B + ((long long)(j0 + r - a.mt) * a.K + kc0) * 2;
-            bulk_copy_g2s(dst + r * GC_RAW_ROW, src, bytes, &raw_full[slot]);
-          }
+        if (lane == 0) {
+          // two 2-D boxes (128-byte swizzle, zero fill outside): mt rows of A, NB of B
+          unsigned char* dst = raw + slot * RAW_BYTES;
+          mbar_arrive_expect_tx(&raw_full[slot], (uint32_t)((a.mt + NB) * 128));
+          tma_load_2d(dst, &map_a, (int)(2 * kc0), i0, &raw_full[slot]);
+          tma_load_2d(dst + a.mt * 128, &map_b, (int)(2 * kc0), j0, &raw_full[slot]);
         }
+        __syncwarp();
         issued = s + 1;
       }
     }
@@ -381,7 +377,7 @@ template <int NB>
 size_t gc_smem() {
   constexpr int B_BYTES = 2 * NB * GC_KB * 4;
   constexpr int OP_BYTES = 2 * GC_A_HALF + B_BYTES;
-  return (size_t)GC_NBUF * OP_BYTES + (size_t)GC_RAW * (64 + NB) * GC_RAW_ROW;
+  return (size_t)GC_NBUF * OP_BYTES + (size_t)GC_RAW * (64 + NB) * 128 + 1024;
 }
 
 int sm_count_dev() {
@@ -422,7 +418,7 @@ GcPlan gc_plan(int ma, int mb, long long K) {
 }
 
 template <int NB>
-void launch_gc(const GcPlan& p, cudaStream_t st, const float* A, const float* B, int ma, int mb,
+int launch_gc(const GcPlan& p, cudaStream_t st, const float* A, const float* B, int ma, int mb,
                long long K, double* part, int* err) {
   GcArgs a;
   a.A = A;
@@ -437,12 +433,17 @@ void launch_gc(const GcPlan& p, cudaStream_t st, const float* A, const float* B,
   a.nit = p.nit;
   a.njt = p.njt;
   a.nk = p.nk;
+  CUtensorMap ma_map, mb_map;
+  if (!ef::make_tmap_2d(&ma_map, A, ma, 2 * K, GC_KB, p.mt, true) ||
+      !ef::make_tmap_2d(&mb_map, B, mb, 2 * K, GC_KB, NB, true))
+    return ef_fail(EF_ERR_CUDA, "gram_tc: tensor map encoding failed");
   const size_t smem = gc_smem<NB>();
   ef::set_smem_once(tc_gram_kernel<NB>, smem);
   long long units = (long long)p.nit * p.njt * p.nk;
   long long grid = sm_count_dev();
   if (grid > units) grid = units;
-  tc_gram_kernel<NB><<<(unsigned)grid, GC_THREADS, smem, st>>>(a);
+  tc_gram_kernel<NB><<<(unsigned)grid, GC_THREADS, smem, st>>>(a, ma_map, mb_map);
+  return EF_OK;
 }
 
 }  // namespace
@@ -464,9 +465,11 @@ extern "C" int ef_gram_tc(const float* A, const float* B, int ma, int mb, long l
   cudaStream_t st = (cudaStream_t)stream;
   const GcPlan p = gc_plan(ma, mb, K);
   ef_count_launches(2);
-  if (p.nb == 16) launch_gc<16>(p, st, A, B, ma, mb, K, (double*)work, err_dev);
-  else if (p.nb == 32) launch_gc<32>(p, st, A, B, ma, mb, K, (double*)work, err_dev);
-  else launch_gc<64>(p, st, A, B, ma, mb, K, (double*)work, err_dev);
+  int rc;
+  if (p.nb == 16) rc = launch_gc<16>(p, st, A, B, ma, mb, K, (double*)work, err_dev);
+  else if (p.nb == 32) rc = launch_gc<32>(p, st, A, B, ma, mb, K, (double*)work, err_dev);
+  else rc = launch_gc<64>(p, st, A, B, ma, mb, K, (double*)work, err_dev);
+  if (rc != EF_OK) return rc;
   const int n = ma * mb;
   tc_gram_reduce_kernel<<<(n + 7) / 8, 256, 0, st>>>((const double2*)work, p.nk, n, (double2*)G);
   return ef_check_launch();

@@ -31,11 +31,11 @@
 #include <cuda.h>
 
 #include <cstdint>
-#include <mutex>
 
 #include "common.cuh"
 #include "status.h"
 #include "tc_common.cuh"
+#include "tmap.h"
 
 namespace {
 
@@ -79,7 +79,8 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_c
   const int N = 2 * a.mp;
   const int kj = a.nch * TR_JC;            // rows of the coefficient operand
   const uint32_t b_half = (uint32_t)N * kj * 4;
-  unsigned char* raw = smem;
+  // TMA box destinations: align the raw ring to 1024 bytes
+  unsigned char* raw = smem + ((1024u - (smem_u32(smem) & 1023u)) & 1023u);
   unsigned char* bops = raw + TR_RAW * TR_RAW_BYTES;
   const uint32_t col_a = (uint32_t)(2 * N);                // first TMEM operand column
   const uint32_t tcols = tmem_cols_for(2 * N + TR_NBUF * 2 * TR_JC);
@@ -295,43 +296,12 @@ int sm_count() {
 }
 
 size_t tr_smem(int nch, int mp) {
-  const size_t s = (size_t)TR_RAW * TR_RAW_BYTES + (size_t)2 * (2 * mp) * (nch * TR_JC) * 4;
+  const size_t s = (size_t)TR_RAW * TR_RAW_BYTES + (size_t)2 * (2 * mp) * (nch * TR_JC) * 4 + 1024;
   return s < (size_t)TR_SMEM_MIN ? (size_t)TR_SMEM_MIN : s;
 }
 
 int chunks_for(int m_in, int m_out, int mode) {
   return (m_in + TR_JC - 1) / TR_JC + (mode != 0 ? (m_out + TR_JC - 1) / TR_JC : 0);
-}
-
-using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiled encode_fn() {
-  static EncodeTiled fn = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiled>(p);
-  });
-  return fn;
-}
-
-// rows x n2 fp32 matrix, boxes of 16 rows x 128 floats, zero fill outside
-bool make_map(CUtensorMap* m, const float* base, int rows, long long n2) {
-  EncodeTiled fn = encode_fn();
-  if (!fn) return false;
-  const cuuint64_t dims[2] = {(cuuint64_t)n2, (cuuint64_t)rows};
-  const cuuint64_t strides[1] = {(cuuint64_t)n2 * 4};
-  const cuuint32_t box[2] = {TR_M, TR_JC};
-  const cuuint32_t estr[2] = {1, 1};
-  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 }  // namespace
@@ -365,7 +335,8 @@ int tc_rotate_launch(const float* C, int ldc, const float* S, float* out, int m_
   a.nch = chunks_for(m_in, m_out, mode);
   a.sign = mode < 0 ? -1.f : 1.f;
   CUtensorMap ms, mo;
-  if (!make_map(&ms, S, m_in, a.n2) || !make_map(&mo, out, m_out, a.n2))
+  if (!make_tmap_2d(&ms, S, m_in, a.n2, TR_M, TR_JC, false) ||
+      !make_tmap_2d(&mo, out, m_out, a.n2, TR_M, TR_JC, false))
     return ef_fail(EF_ERR_CUDA, "rotate: tensor map encoding failed");
   const size_t smem = tr_smem(a.nch, a.mp);
   ef::set_smem_once(tc_rotate_kernel, smem);
