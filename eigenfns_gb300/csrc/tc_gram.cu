@@ -16,10 +16,13 @@
 // and units (K-chunks) are reduced in fp64.
 //
 // A persistent CTA (448 threads) walks work units (A-tile, B-tile, K-chunk):
-//   warp 13      loads: one bulk copy (TMA engine) per row and stage into a 4-deep
-//                raw ring (mbarrier byte counts);
-//   warps 0-7    converters: hi/lo split (and the A' swap) of the raw stage, 16-byte
-//                stores into a 3-deep ring of K-major operand stages;
+//   warp 13      loads: per 16-complex stage one 2-D TMA box of the unit's A rows and
+//                one of its B rows (128-byte swizzle, zero fill outside) into a raw
+//                shared-memory ring;
+//   warps 0-3    A rows: one TMEM lane (an A or A' row) per thread, hi/lo split and
+//                tcgen05.st into a ring of TMEM operand stages (the MMA's A operand
+//                lives in TMEM);
+//   warps 4-7    B rows: hi/lo split into a ring of K-major shared-memory stages;
 //   warp 12      one thread issues each stage's MMAs and commits them;
 //   warps 8-11   drain finished segments (one TMEM lane per thread, all columns)
 //                and write the unit's partial sums.
@@ -42,17 +45,17 @@ namespace {
 using namespace ef::tc;
 
 constexpr int GC_THREADS = 448;
-constexpr int GC_CONV = 256;          // converter threads (warps 0-7)
+constexpr int GC_CONV = 256;          // converter threads: warps 0-3 A rows, 4-7 B rows
 constexpr int GC_MMA_WARP = 12;
 constexpr int GC_LOAD_WARP = 13;
 constexpr int GC_KB = 32;             // reals per stage (16 complex) = 4 k-steps of 8
-constexpr int GC_NBUF = 3;            // operand stages
-constexpr int GC_RAW = 4;             // raw stages per converter thread
+constexpr int GC_NBUF = 3;            // operand stages (TMEM A, shared B)
+constexpr int GC_RAW = 6;             // raw box stages
 constexpr int GC_SEG = 8;             // stages per TMEM accumulation segment
-constexpr int GC_A_HALF = 128 * GC_KB * 4;   // 16 KB: A_hi or A_lo of one stage
+constexpr int GC_SMEM_MIN = 120 * 1024;   // keeps one CTA (and its TMEM) per SM
 
-// byte offset of (row r, k-quad q) in an operand tile: core matrices of 8 rows x 16 B,
-// K-adjacent core matrices 128 B apart, 8-row groups (GC_KB/4)*128 = 1024 B apart
+// byte offset of (row r, k-quad q) in a K-major operand tile: core matrices of 8 rows
+// x 16 B, K-adjacent core matrices 128 B apart, 8-row groups (GC_KB/4)*128 = 1024 B apart
 __device__ __forceinline__ int quad_off(int r, int q) {
   return (((r >> 3) * (GC_KB / 4) + q) << 7) + ((r & 7) << 4);
 }
@@ -62,8 +65,6 @@ __device__ __forceinline__ uint64_t gram_desc(uint32_t addr) {
 }
 
 struct GcArgs {
-  const float* A;
-  const float* B;
   double* partial;      // entry-major (ma*mb, nk) double2
   int* err;
   long long K;          // complex values per row
@@ -75,10 +76,11 @@ struct GcArgs {
 template <int NB>
 __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_constant__ CUtensorMap map_a,
                                                 const __grid_constant__ CUtensorMap map_b) {
-  constexpr int B_BYTES = 2 * NB * GC_KB * 4;                  // [B_hi; B_lo]
-  constexpr int OP_BYTES = 2 * GC_A_HALF + B_BYTES;
-  constexpr int IPT = ((64 + NB) * (GC_KB / 4) + GC_CONV - 1) / GC_CONV;   // items per thread
+  constexpr int B_BYTES = 2 * NB * GC_KB * 4;                  // [B_hi; B_lo] per stage
   constexpr int RAW_BYTES = (64 + NB) * 128;                   // A box + B box, 128-B rows
+  constexpr int IPB = NB * (GC_KB / 4) / 128;                  // B items per B-converter thread
+  constexpr uint32_t COL_A = 4 * NB;                           // first TMEM operand column
+  constexpr uint32_t TCOLS = tmem_cols_for(4 * NB + GC_NBUF * 2 * GC_KB);
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t op_full[GC_NBUF], op_empty[GC_NBUF];
   __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done_bar;
@@ -89,9 +91,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // raw boxes use the 128-byte swizzle, which wants 1024-byte aligned stages
   unsigned char* raw = smem + ((1024u - (smem_u32(smem) & 1023u)) & 1023u);
-  unsigned char* ops = raw + GC_RAW * RAW_BYTES;
-  constexpr uint32_t TCOLS = tmem_cols_for(4 * NB);
-  const int nitems = (a.mt + NB) * (GC_KB / 4);                // items per stage
+  unsigned char* bst = raw + GC_RAW * RAW_BYTES;
   const long long units = (long long)a.nit * a.njt * a.nk;
   const long long my_units = units > blockIdx.x ? (units - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
 
@@ -112,10 +112,6 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // operand rows the converters never write (A rows >= 2*mt) must read as zero
-  for (int e = tid; e < GC_NBUF * OP_BYTES / 16; e += GC_THREADS)
-    reinterpret_cast<float4*>(ops)[e] = make_float4(0.f, 0.f, 0.f, 0.f);
-  fence_async_smem();
   if (warp == GC_MMA_WARP) tmem_alloc(&tmem_base_s, TCOLS);
   fence_before_sync();
   __syncthreads();
@@ -137,17 +133,18 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
 
   if (warp < 8) {
     // ---------------- converters ----------------
-    // item e -> row r = e % rows, quad q = e / rows: consecutive threads take consecutive
-    // rows, so the raw reads (rows padded to 144 B) and the 16-byte operand stores are
-    // conflict-free. Rows outside the matrices and quads past the unit's end read zero.
-    const int rows = a.mt + NB;
-    int cr[IPT], cq[IPT];
-#pragma unroll
-    for (int u = 0; u < IPT; ++u) {
-      const int e = tid + u * GC_CONV;
-      cr[u] = e % rows;
-      cq[u] = e / rows;
-    }
+    // warps 0-3: TMEM lane L = 32*warp + lane is A row L (L < mt) or A' row L - mt
+    // (mt <= L < 2mt); its 32 reals of the stage come from the swizzled A box.
+    // warps 4-7: B item e -> row e % NB, quad e / NB (consecutive threads, consecutive
+    // rows: conflict-free swizzled reads and operand stores).
+    // Quads past the unit's end read zero (boxes past the matrix are zero-filled).
+    const bool arow = warp < 4;
+    const int L = warp * 32 + lane;
+    const bool aprime = arow && L >= a.mt;
+    const int ar = aprime ? L - a.mt : L;
+    const bool aact = arow && L < 2 * a.mt;
+    const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+    const int bt = tid - 128;
     long long s = 0;
     for (long long k = 0; k < my_units && !abort_s; ++k) {
       int it, jt, kc, nst;
@@ -155,7 +152,6 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
       unit_of(k, it, jt, kc, kbeg, nst);
       long long kend = kbeg + a.kchunk;
       if (kend > a.K) kend = a.K;
-      const int mrows = a.ma - it * a.mt, nrows = a.mb - jt * NB;
       for (int st = 0; st < nst; ++st, ++s) {
         const int slot = (int)(s % GC_RAW);
         if (!mbar_wait(&raw_full[slot], (uint32_t)((s / GC_RAW) & 1))) {
@@ -165,49 +161,70 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
         }
         const long long kc0 = kbeg + (long long)st * (GC_KB / 2);
         const unsigned char* rs = raw + slot * RAW_BYTES;
-        float4 v[IPT];
-#pragma unroll
-        for (int u = 0; u < IPT; ++u) {
-          const int e = tid + u * GC_CONV;
-          const int r = cr[u];
-          const bool rin = r < a.mt ? r < mrows : r - a.mt < nrows;
-          v[u] = (e < nitems && rin && kc0 + 2 * cq[u] < kend)
-                     ? *reinterpret_cast<const float4*>(rs + r * 128 + ((cq[u] ^ (r & 7)) << 4))
-                     : make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-        mbar_arrive(&raw_empty[slot]);
         const int o = (int)(s % GC_NBUF);
-        if (!mbar_wait(&op_empty[o], (uint32_t)(((s / GC_NBUF) + 1) & 1))) {
-          abort_s = 1;
-          atomicExch(a.err, 1);
-          break;
-        }
-        unsigned char* base = ops + o * OP_BYTES;
+        if (arow) {
+          float h[32], l[32];
 #pragma unroll
-        for (int u = 0; u < IPT; ++u) {
-          const int e = tid + u * GC_CONV;
-          if (e < nitems) {
-            const int r = cr[u], q = cq[u];
-            const float4 x = v[u];
-            const float4 h = make_float4(tf32_rn(x.x), tf32_rn(x.y), tf32_rn(x.z), tf32_rn(x.w));
-            const float4 l = make_float4(tf32_rn(x.x - h.x), tf32_rn(x.y - h.y), tf32_rn(x.z - h.z),
-                                         tf32_rn(x.w - h.w));
-            if (r < a.mt) {
-              *reinterpret_cast<float4*>(base + quad_off(r, q)) = h;
-              *reinterpret_cast<float4*>(base + GC_A_HALF + quad_off(r, q)) = l;
-              // A' = (-ai, ar) per complex: swap within the pairs and negate the new real part
-              *reinterpret_cast<float4*>(base + quad_off(a.mt + r, q)) = make_float4(-h.y, h.x, -h.w, h.z);
-              *reinterpret_cast<float4*>(base + GC_A_HALF + quad_off(a.mt + r, q)) =
-                  make_float4(-l.y, l.x, -l.w, l.z);
-            } else {
-              const int rb = r - a.mt;
-              *reinterpret_cast<float4*>(base + 2 * GC_A_HALF + quad_off(rb, q)) = h;
-              *reinterpret_cast<float4*>(base + 2 * GC_A_HALF + quad_off(NB + rb, q)) = l;
-            }
+          for (int q = 0; q < 8; ++q) {
+            float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (aact && kc0 + 2 * q < kend)
+              x = *reinterpret_cast<const float4*>(rs + ar * 128 + ((q ^ (ar & 7)) << 4));
+            if (aprime) x = make_float4(-x.y, x.x, -x.w, x.z);   // (-ai, ar) per complex
+            h[4 * q] = x.x;
+            h[4 * q + 1] = x.y;
+            h[4 * q + 2] = x.z;
+            h[4 * q + 3] = x.w;
           }
+          mbar_arrive(&raw_empty[slot]);
+#pragma unroll
+          for (int e = 0; e < 32; ++e) {
+            const float hv = tf32_rn(h[e]);
+            l[e] = tf32_rn(h[e] - hv);
+            h[e] = hv;
+          }
+          if (!mbar_wait(&op_empty[o], (uint32_t)(((s / GC_NBUF) + 1) & 1))) {
+            abort_s = 1;
+            atomicExch(a.err, 1);
+            break;
+          }
+          fence_after_sync();
+          const uint32_t col = COL_A + (uint32_t)(o * 2 * GC_KB);
+          tmem_st32(lane_base + col, h);
+          tmem_st32(lane_base + col + GC_KB, l);
+          tmem_wait_st();
+          fence_before_sync();
+          mbar_arrive(&op_full[o]);
+        } else {
+          float4 v[IPB];
+#pragma unroll
+          for (int u = 0; u < IPB; ++u) {
+            const int e = bt + u * 128;
+            const int rb = e % NB, q = e / NB;
+            v[u] = (kc0 + 2 * q < kend)
+                       ? *reinterpret_cast<const float4*>(rs + (a.mt + rb) * 128 + ((q ^ (rb & 7)) << 4))
+                       : make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+          mbar_arrive(&raw_empty[slot]);
+          if (!mbar_wait(&op_empty[o], (uint32_t)(((s / GC_NBUF) + 1) & 1))) {
+            abort_s = 1;
+            atomicExch(a.err, 1);
+            break;
+          }
+          unsigned char* base = bst + o * B_BYTES;
+#pragma unroll
+          for (int u = 0; u < IPB; ++u) {
+            const int e = bt + u * 128;
+            const int rb = e % NB, q = e / NB;
+            const float4 x = v[u];
+            const float4 hh = make_float4(tf32_rn(x.x), tf32_rn(x.y), tf32_rn(x.z), tf32_rn(x.w));
+            const float4 ll = make_float4(tf32_rn(x.x - hh.x), tf32_rn(x.y - hh.y), tf32_rn(x.z - hh.z),
+                                          tf32_rn(x.w - hh.w));
+            *reinterpret_cast<float4*>(base + quad_off(rb, q)) = hh;
+            *reinterpret_cast<float4*>(base + quad_off(NB + rb, q)) = ll;
+          }
+          fence_async_smem();
+          mbar_arrive(&op_full[o]);
         }
-        fence_async_smem();
-        mbar_arrive(&op_full[o]);
       }
     }
   } else if (warp < 12) {
@@ -261,7 +278,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
   } else if (warp == GC_MMA_WARP && lane == 0) {
     // ---------------- MMA issue ----------------
     const uint32_t id1 = idesc_tf32(128, 2 * NB), id2 = idesc_tf32(128, NB);
-    const uint64_t desc0 = gram_desc(smem_u32(ops));
+    const uint64_t bdesc0 = gram_desc(smem_u32(bst));
     long long s = 0, q = 0;
     bool issued = false;
     for (long long k = 0; k < my_units && !abort_s; ++k) {
@@ -285,14 +302,14 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
         }
         fence_after_sync();
         const uint32_t d = tmem + (uint32_t)(ab * 2 * NB);
+        const uint32_t a_hi = tmem + COL_A + (uint32_t)(o * 2 * GC_KB), a_lo = a_hi + GC_KB;
         // descriptors differ from the base one only in the start-address field
-        const uint64_t aHi = desc0 + (uint64_t)((o * OP_BYTES) >> 4);
-        const uint64_t aLo = aHi + (uint64_t)(GC_A_HALF >> 4), bB = aHi + (uint64_t)((2 * GC_A_HALF) >> 4);
+        const uint64_t bB = bdesc0 + (uint64_t)((o * B_BYTES) >> 4);
 #pragma unroll
         for (int g = 0; g < GC_KB / 8; ++g) {
           const uint64_t off = (uint64_t)(g * 256 >> 4);
-          mma_tf32(d, aHi + off, bB + off, id1, (seg_first && g == 0) ? 0u : 1u);
-          mma_tf32(d + NB, aLo + off, bB + off, id2, 1u);
+          mma_tf32_ts(d, a_hi + 8 * g, bB + off, id1, (seg_first && g == 0) ? 0u : 1u);
+          mma_tf32_ts(d + NB, a_lo + 8 * g, bB + off, id2, 1u);
         }
         mma_commit(&op_empty[o]);
         issued = true;
@@ -306,8 +323,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
       mma_commit(&done_bar);
       mbar_wait(&done_bar, 0);
     }
-  }
-  if (warp == GC_LOAD_WARP) {
+  } else if (warp == GC_LOAD_WARP && lane == 0) {
     // ---------------- loader ----------------
     // per stage one 2-D box of the unit's A rows and one of its B rows (16 complex =
     // 128 B per row), counted on raw_full in bytes
@@ -319,31 +335,22 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
       const int i0 = it * a.mt, j0 = jt * NB;
       for (int st = 0; st < nst; ++st, ++s) {
         const int slot = (int)(s % GC_RAW);
-        bool ok = true;
-        if (lane == 0) ok = mbar_wait(&raw_empty[slot], (uint32_t)(((s / GC_RAW) + 1) & 1));
-        if (!__shfl_sync(0xffffffffu, ok ? 1 : 0, 0)) {
-          if (lane == 0) {
-            abort_s = 1;
-            atomicExch(a.err, 1);
-          }
+        if (!mbar_wait(&raw_empty[slot], (uint32_t)(((s / GC_RAW) + 1) & 1))) {
+          abort_s = 1;
+          atomicExch(a.err, 1);
           break;
         }
         const long long kc0 = kbeg + (long long)st * (GC_KB / 2);
-        if (lane == 0) {
-          // two 2-D boxes (128-byte swizzle, zero fill outside): mt rows of A, NB of B
-          unsigned char* dst = raw + slot * RAW_BYTES;
-          mbar_arrive_expect_tx(&raw_full[slot], (uint32_t)((a.mt + NB) * 128));
-          tma_load_2d(dst, &map_a, (int)(2 * kc0), i0, &raw_full[slot]);
-          tma_load_2d(dst + a.mt * 128, &map_b, (int)(2 * kc0), j0, &raw_full[slot]);
-        }
-        __syncwarp();
+        unsigned char* dst = raw + slot * RAW_BYTES;
+        mbar_arrive_expect_tx(&raw_full[slot], (uint32_t)((a.mt + NB) * 128));
+        tma_load_2d(dst, &map_a, (int)(2 * kc0), i0, &raw_full[slot]);
+        tma_load_2d(dst + a.mt * 128, &map_b, (int)(2 * kc0), j0, &raw_full[slot]);
         issued = s + 1;
       }
     }
     // no copy may still be landing when the CTA exits: wait for the last issued phases
-    if (lane == 0)
-      for (long long t = issued - GC_RAW > 0 ? issued - GC_RAW : 0; t < issued; ++t)
-        mbar_wait(&raw_full[(int)(t % GC_RAW)], (uint32_t)((t / GC_RAW) & 1));
+    for (long long t = issued - GC_RAW > 0 ? issued - GC_RAW : 0; t < issued; ++t)
+      mbar_wait(&raw_full[(int)(t % GC_RAW)], (uint32_t)((t / GC_RAW) & 1));
   }
   fence_before_sync();
   __syncthreads();
@@ -375,9 +382,8 @@ int tc_nb(int mb) { return mb <= 16 ? 16 : (mb <= 32 ? 32 : 64); }
 
 template <int NB>
 size_t gc_smem() {
-  constexpr int B_BYTES = 2 * NB * GC_KB * 4;
-  constexpr int OP_BYTES = 2 * GC_A_HALF + B_BYTES;
-  return (size_t)GC_NBUF * OP_BYTES + (size_t)GC_RAW * (64 + NB) * 128 + 1024;
+  const size_t s = (size_t)GC_NBUF * 2 * NB * GC_KB * 4 + (size_t)GC_RAW * (64 + NB) * 128 + 1024;
+  return s < (size_t)GC_SMEM_MIN ? (size_t)GC_SMEM_MIN : s;
 }
 
 int sm_count_dev() {
@@ -421,8 +427,6 @@ template <int NB>
 int launch_gc(const GcPlan& p, cudaStream_t st, const float* A, const float* B, int ma, int mb,
                long long K, double* part, int* err) {
   GcArgs a;
-  a.A = A;
-  a.B = B;
   a.partial = part;
   a.err = err;
   a.K = K;
