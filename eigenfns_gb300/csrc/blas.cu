@@ -690,7 +690,11 @@ int noalloc_scratch(void** out) {
 }
 }  // namespace
 
+// ef_gram runs on the tensor cores (ef_gram_tc) unless EF_GRAM_KERNEL selects otherwise
+constexpr bool kGramTensorCoreDefault = false;
+
 namespace ef {
+int* tc_error_dev();
 int tc_rotate_max_rows(int m_out, int mode);
 int tc_rotate_launch(const float* C, int ldc, const float* S, float* out, int m_in, int m_out,
                      long long K, int mode, cudaStream_t st);
@@ -700,7 +704,9 @@ extern "C" {
 
 size_t ef_gram_workspace_bytes(int ma, int mb, long long K) {
   if (ma <= 0 || mb <= 0 || K <= 0) return 0;
-  return (size_t)gram_splits(ma, mb, K) * ma * mb * sizeof(double2) + 256;
+  const size_t simt = (size_t)gram_splits(ma, mb, K) * ma * mb * sizeof(double2) + 256;
+  const size_t tc = ef_gram_tc_workspace_bytes(ma, mb, K);
+  return simt > tc ? simt : tc;
 }
 
 int ef_gram(const float* A, const float* B, int ma, int mb, long long K, double* G, void* work,
@@ -709,12 +715,15 @@ int ef_gram(const float* A, const float* B, int ma, int mb, long long K, double*
   if (!work || work_bytes < ef_gram_workspace_bytes(ma, mb, K))
     return ef_fail(EF_ERR_WORKSPACE, "gram work buffer too small");
   cudaStream_t st = (cudaStream_t)stream;
+  const bool pipe = (K % 2 == 0) && ((((uintptr_t)A) | ((uintptr_t)B)) % 16 == 0);
+  const char* kern = getenv("EF_GRAM_KERNEL");
+  const bool tc = kern ? strcmp(kern, "tc") == 0 : kGramTensorCoreDefault;
+  if (tc && pipe) return ef_gram_tc(A, B, ma, mb, K, G, ef::tc_error_dev(), work, work_bytes, stream);
   int ns = gram_splits(ma, mb, K);
   long long kchunk = (K + ns - 1) / ns;
   kchunk = (kchunk + GBK - 1) / GBK * GBK;
   ns = (int)((K + kchunk - 1) / kchunk);
   dim3 grid((ma + GT - 1) / GT, (mb + GT - 1) / GT, ns);
-  const bool pipe = (K % 2 == 0) && ((((uintptr_t)A) | ((uintptr_t)B)) % 16 == 0);
   ef_count_launches(1);
   if (pipe)
     gram_pipe_kernel<<<grid, PG_THREADS, 0, st>>>((const float2*)A, (const float2*)B, ma, mb, K,

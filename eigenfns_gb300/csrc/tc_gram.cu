@@ -49,8 +49,7 @@ constexpr int GC_CONV = 256;          // converter threads: warps 0-3 A rows, 4-
 constexpr int GC_MMA_WARP = 12;
 constexpr int GC_LOAD_WARP = 13;
 constexpr int GC_KB = 32;             // reals per stage (16 complex) = 4 k-steps of 8
-constexpr int GC_NBUF = 3;            // operand stages (TMEM A, shared B)
-constexpr int GC_RAW = 6;             // raw box stages
+constexpr int GC_RAW = 8;             // raw box stages
 constexpr int GC_SEG = 8;             // stages per TMEM accumulation segment
 constexpr int GC_SMEM_MIN = 120 * 1024;   // keeps one CTA (and its TMEM) per SM
 
@@ -72,10 +71,17 @@ struct GcArgs {
   int ma, mb, mt, nit, njt, nk;
 };
 
+// operand stages (TMEM A, shared B): what TMEM holds after the two accumulators
+template <int NB>
+__host__ __device__ constexpr int gc_nbuf() {
+  return (512 - 4 * NB) / (2 * GC_KB) > 6 ? 6 : (512 - 4 * NB) / (2 * GC_KB);
+}
+
 // 14 warps: at most 4 per SM sub-partition, so 128 registers a thread fit
 template <int NB>
 __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_constant__ CUtensorMap map_a,
                                                 const __grid_constant__ CUtensorMap map_b) {
+  constexpr int GC_NBUF = gc_nbuf<NB>();
   constexpr int B_BYTES = 2 * NB * GC_KB * 4;                  // [B_hi; B_lo] per stage
   constexpr int RAW_BYTES = (64 + NB) * 128;                   // A box + B box, 128-B rows
   constexpr int IPB = NB * (GC_KB / 4) / 128;                  // B items per B-converter thread
@@ -382,7 +388,7 @@ int tc_nb(int mb) { return mb <= 16 ? 16 : (mb <= 32 ? 32 : 64); }
 
 template <int NB>
 size_t gc_smem() {
-  const size_t s = (size_t)GC_NBUF * 2 * NB * GC_KB * 4 + (size_t)GC_RAW * (64 + NB) * 128 + 1024;
+  const size_t s = (size_t)gc_nbuf<NB>() * 2 * NB * GC_KB * 4 + (size_t)GC_RAW * (64 + NB) * 128 + 1024;
   return s < (size_t)GC_SMEM_MIN ? (size_t)GC_SMEM_MIN : s;
 }
 

@@ -48,7 +48,7 @@ constexpr int TR_MMA_WARP = 12;
 constexpr int TR_LOAD_WARP = 13;
 constexpr int TR_M = 128;                 // real positions per tile
 constexpr int TR_JC = 16;                 // rows of S per stage
-constexpr int TR_NBUF = 4;                // TMEM operand stages (hi + lo: 2*TR_JC columns each)
+constexpr int TR_NBUF_MAX = 8;            // TMEM operand stages (hi + lo: 2*TR_JC columns each)
 constexpr int TR_RAW = 12;                // raw shared-memory stages
 constexpr int TR_RAW_BYTES = TR_JC * TR_M * 4;     // 8 KB per raw stage (row-major box)
 constexpr int TR_SMEM_MAX = 227 * 1024 - 1024;   // dynamic part; static barriers take the rest
@@ -61,7 +61,7 @@ struct TrArgs {
   float* out;           // m_out rows of n2 floats
   long long n2;         // 2K
   long long ntiles;
-  int ldc, m_in, m_out, mp, ncs, nch;
+  int ldc, m_in, m_out, mp, ncs, nch, nbuf;
   float sign;           // -1 for subtraction
 };
 
@@ -69,7 +69,7 @@ struct TrArgs {
 __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_constant__ CUtensorMap map_s,
                                                   const __grid_constant__ CUtensorMap map_o) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(8) uint64_t op_full[TR_NBUF], op_empty[TR_NBUF];
+  __shared__ __align__(8) uint64_t op_full[TR_NBUF_MAX], op_empty[TR_NBUF_MAX];
   __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done_bar;
   __shared__ __align__(8) uint64_t raw_full[TR_RAW], raw_empty[TR_RAW];
   __shared__ uint32_t tmem_base_s;
@@ -83,11 +83,11 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_c
   unsigned char* raw = smem + ((1024u - (smem_u32(smem) & 1023u)) & 1023u);
   unsigned char* bops = raw + TR_RAW * TR_RAW_BYTES;
   const uint32_t col_a = (uint32_t)(2 * N);                // first TMEM operand column
-  const uint32_t tcols = tmem_cols_for(2 * N + TR_NBUF * 2 * TR_JC);
+  const uint32_t tcols = tmem_cols_for(2 * N + a.nbuf * 2 * TR_JC);
 
   if (tid == 0) {
     abort_s = 0;
-    for (int b = 0; b < TR_NBUF; ++b) {
+    for (int b = 0; b < a.nbuf; ++b) {
       mbar_init(&op_full[b], TR_CONV);
       mbar_init(&op_empty[b], 1);
     }
@@ -140,6 +140,8 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_c
     const int q4 = warp & 3, hv = warp >> 2;
     const int p = q4 * 32 + lane;
     const uint32_t lane_base = tmem + ((uint32_t)(q4 * 32) << 16);
+    int o = 0;
+    uint32_t uo = 0;                                   // operand ring slot and its use count
     for (long long s = 0; s < nstages; ++s) {
       const int slot = (int)(s % TR_RAW);
       if (abort_s) break;
@@ -157,8 +159,7 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_c
         lo[r] = tf32_rn(x - hi[r]);
       }
       mbar_arrive(&raw_empty[slot]);
-      const int o = (int)(s % TR_NBUF);
-      if (!mbar_wait(&op_empty[o], (uint32_t)(((s / TR_NBUF) + 1) & 1))) {
+      if (!mbar_wait(&op_empty[o], (uo + 1) & 1)) {
         abort_s = 1;
         atomicExch(&g_tc_error, 1);
         break;
@@ -170,6 +171,10 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_c
       tmem_wait_st();
       fence_before_sync();
       mbar_arrive(&op_full[o]);
+      if (++o == a.nbuf) {
+        o = 0;
+        ++uo;
+      }
     }
   } else if (warp < 12) {
     // ---------------- epilogue ----------------
@@ -207,6 +212,8 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_c
     const uint32_t idesc = idesc_tf32(TR_M, N);
     const uint64_t b_desc0 = smem_desc(smem_u32(bops), 128, (uint32_t)kq * 128);
     bool issued = false;
+    int o = 0;
+    uint32_t uo = 0;                                   // operand ring slot and its use count
     for (long long k = 0; k < my_tiles && !abort_s; ++k) {
       const int ab = (int)(k & 1);
       if (!mbar_wait(&acc_empty[ab], (uint32_t)(((k >> 1) + 1) & 1))) {
@@ -217,9 +224,7 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_c
       fence_after_sync();
       const uint32_t d = tmem + (uint32_t)(ab * N);
       for (int c = 0; c < a.nch; ++c) {
-        const long long s = k * a.nch + c;
-        const int o = (int)(s % TR_NBUF);
-        if (!mbar_wait(&op_full[o], (uint32_t)((s / TR_NBUF) & 1))) {
+        if (!mbar_wait(&op_full[o], uo & 1)) {
           abort_s = 1;
           atomicExch(&g_tc_error, 1);
           break;
@@ -237,6 +242,10 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_c
         }
         mma_commit(&op_empty[o]);
         issued = true;
+        if (++o == a.nbuf) {
+          o = 0;
+          ++uo;
+        }
       }
       if (abort_s) break;
       mma_commit(&acc_full[ab]);
@@ -334,6 +343,8 @@ int tc_rotate_launch(const float* C, int ldc, const float* S, float* out, int m_
   a.ncs = (m_in + TR_JC - 1) / TR_JC;
   a.nch = chunks_for(m_in, m_out, mode);
   a.sign = mode < 0 ? -1.f : 1.f;
+  a.nbuf = (512 - 2 * 2 * a.mp) / (2 * TR_JC);          // TMEM left after the accumulators
+  if (a.nbuf > TR_NBUF_MAX) a.nbuf = TR_NBUF_MAX;
   CUtensorMap ms, mo;
   if (!make_tmap_2d(&ms, S, m_in, a.n2, TR_M, TR_JC, false) ||
       !make_tmap_2d(&mo, out, m_out, a.n2, TR_M, TR_JC, false))
@@ -345,6 +356,13 @@ int tc_rotate_launch(const float* C, int ldc, const float* S, float* out, int m_
   ef_count_launches(1);
   tc_rotate_kernel<<<(unsigned)grid, TR_THREADS, smem, st>>>(a, ms, mo);
   return ef_check_launch();
+}
+
+// device address of the tensor-core kernels' error flag (current device)
+int* tc_error_dev() {
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_tc_error) != cudaSuccess) return nullptr;
+  return (int*)p;
 }
 
 // reads and clears the tensor-core kernels' device error flag (synchronises the device)
