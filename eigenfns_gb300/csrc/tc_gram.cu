@@ -4,27 +4,28 @@
 // products over the interleaved (re, im) storage:
 //   Re G = A_r . B_r^T            A_r[i] = (ar0, ai0, ar1, ai1, ...)
 //   Im G = A'_r . B_r^T           A'_r[i] = (-ai0, ar0, -ai1, ar1, ...)
-// Three TF32 products per pair give fp32-class products (x = hi + lo). The M = 128
-// lanes of one MMA hold 32 rows of A four ways, [A_hi; A'_hi; A_lo; A'_lo], and the N
-// operand holds NB rows of B as [B_hi; B_lo], so ONE MMA per 8-real k-step gives
-//   lanes  0..63: hh | hl        lanes 64..127: lh | (ll, unused)
-// and Re/Im G = hh + hl + lh. Lanes of the hi and lo halves write separate partial
-// sums, which the fp64 reduction adds with the K-chunks.
+// The M = 128 operand holds up to MT (32 or 64) rows of A in rows [0, MT) and the
+// matching rows of A' in [MT, 2MT); the N operand holds NB rows of B as
+// [B_hi; B_lo]. Per 8-real k-step two MMAs give fp32-class products (x = hi + lo):
+//   D[:, 0:2NB]  += A_hi [B_hi; B_lo]^T      (hh | hl)
+//   D[:, NB:2NB] += A_lo B_hi^T              (hl + lh)
 // Tensor-core fp32 accumulation is not round-to-nearest over long chains, so the
 // accumulation is cut into segments of SEG stages, alternating between two TMEM
 // accumulators; each finished segment is read back (tcgen05.ld) and added into fp32
-// registers while the next segment's MMAs run; a work unit's sums go out in fp64.
+// registers while the next segment's MMAs run; a work unit's sum goes out in fp64
+// and units (K-chunks) are reduced in fp64.
 //
 // A persistent CTA (448 threads) walks work units (A-tile, B-tile, K-chunk):
-//   warp 13      loads: per 16-complex stage one 2-D TMA box of the unit's 32 A rows
-//                and one of its B rows (128-byte swizzle, zero fill outside) into a
-//                raw shared-memory ring;
-//   warps 0-3    A rows: one TMEM lane per thread (row, hi or lo, A or A'), split and
-//                tcgen05.st into a ring of TMEM operand stages (A lives in TMEM);
+//   warp 13      loads: per 16-complex stage one 2-D TMA box of the unit's A rows and
+//                one of its B rows (128-byte swizzle, zero fill outside) into a raw
+//                shared-memory ring;
+//   warps 0-3    A rows: one TMEM lane (an A or A' row) per thread, hi/lo split and
+//                tcgen05.st into a ring of TMEM operand stages (the MMA's A operand
+//                lives in TMEM);
 //   warps 4-7    B rows: hi/lo split into a ring of K-major shared-memory stages;
 //   warp 12      one thread issues each stage's MMAs and commits them;
-//   warps 8-11   drain finished segments (one TMEM lane per thread) and write the
-//                unit's partial sums.
+//   warps 8-11   drain finished segments (one TMEM lane per thread, all columns)
+//                and write the unit's partial sums.
 // Every mbarrier wait is bounded; on timeout the kernel sets the error flag, stops,
 // waits (bounded) for its own copies and MMAs and frees its TMEM.
 //
@@ -47,7 +48,6 @@ constexpr int GC_THREADS = 448;
 constexpr int GC_CONV = 256;          // converter threads: warps 0-3 A rows, 4-7 B rows
 constexpr int GC_MMA_WARP = 12;
 constexpr int GC_LOAD_WARP = 13;
-constexpr int GC_MT = 32;             // A rows per tile
 constexpr int GC_KB = 32;             // reals per stage (16 complex) = 4 k-steps of 8
 constexpr int GC_RAW = 8;             // raw box stages
 constexpr int GC_SEG = 8;             // stages per TMEM accumulation segment
@@ -63,32 +63,32 @@ __device__ __forceinline__ uint64_t gram_desc(uint32_t addr) {
   return smem_desc(addr, 128, (GC_KB / 4) * 128);
 }
 
-// operand stages (TMEM A, shared B): what TMEM holds after the two accumulators
-template <int NB>
-__host__ __device__ constexpr int gc_nbuf() {
-  return (512 - 4 * NB) / GC_KB > 8 ? 8 : (512 - 4 * NB) / GC_KB;
-}
-
 struct GcArgs {
-  double* partial;      // entry-major (ma*mb, 2*nk) double2
+  double* partial;      // entry-major (ma*mb, nk) double2
   int* err;
   long long K;          // complex values per row
   long long kchunk;     // complex values per unit (multiple of 16)
-  int ma, mb, nit, njt, nk;
+  int ma, mb, mt, nit, njt, nk;
 };
+
+// operand stages (TMEM A, shared B): what TMEM holds after the two accumulators
+template <int NB>
+__host__ __device__ constexpr int gc_nbuf() {
+  return (512 - 4 * NB) / (2 * GC_KB) > 6 ? 6 : (512 - 4 * NB) / (2 * GC_KB);
+}
 
 // 14 warps: at most 4 per SM sub-partition, so 128 registers a thread fit
 template <int NB>
 __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_constant__ CUtensorMap map_a,
                                                 const __grid_constant__ CUtensorMap map_b) {
-  constexpr int NBUF = gc_nbuf<NB>();
+  constexpr int GC_NBUF = gc_nbuf<NB>();
   constexpr int B_BYTES = 2 * NB * GC_KB * 4;                  // [B_hi; B_lo] per stage
-  constexpr int RAW_BYTES = (GC_MT + NB) * 128;                // A box + B box, 128-B rows
+  constexpr int RAW_BYTES = (64 + NB) * 128;                   // A box + B box, 128-B rows
   constexpr int IPB = NB * (GC_KB / 4) / 128;                  // B items per B-converter thread
   constexpr uint32_t COL_A = 4 * NB;                           // first TMEM operand column
-  constexpr uint32_t TCOLS = tmem_cols_for(4 * NB + NBUF * GC_KB);
+  constexpr uint32_t TCOLS = tmem_cols_for(4 * NB + GC_NBUF * 2 * GC_KB);
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(8) uint64_t op_full[NBUF], op_empty[NBUF];
+  __shared__ __align__(8) uint64_t op_full[GC_NBUF], op_empty[GC_NBUF];
   __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done_bar;
   __shared__ __align__(8) uint64_t raw_full[GC_RAW], raw_empty[GC_RAW];
   __shared__ uint32_t tmem_base_s;
@@ -103,7 +103,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
 
   if (tid == 0) {
     abort_s = 0;
-    for (int b = 0; b < NBUF; ++b) {
+    for (int b = 0; b < GC_NBUF; ++b) {
       mbar_init(&op_full[b], GC_CONV);
       mbar_init(&op_empty[b], 1);
     }
@@ -139,19 +139,19 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
 
   if (warp < 8) {
     // ---------------- converters ----------------
-    // warps 0-3: TMEM lane L = 32*warp + lane holds A row (L & 31): lanes 0-31 A_hi,
-    // 32-63 A'_hi, 64-95 A_lo, 96-127 A'_lo; its 32 reals come from the swizzled A box.
+    // warps 0-3: TMEM lane L = 32*warp + lane is A row L (L < mt) or A' row L - mt
+    // (mt <= L < 2mt); its 32 reals of the stage come from the swizzled A box.
     // warps 4-7: B item e -> row e % NB, quad e / NB (consecutive threads, consecutive
     // rows: conflict-free swizzled reads and operand stores).
     // Quads past the unit's end read zero (boxes past the matrix are zero-filled).
     const bool arow = warp < 4;
-    const int ar = lane;
-    const bool aprime = (warp & 1) != 0, alo = warp >= 2;
+    const int L = warp * 32 + lane;
+    const bool aprime = arow && L >= a.mt;
+    const int ar = aprime ? L - a.mt : L;
+    const bool aact = arow && L < 2 * a.mt;
     const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
     const int bt = tid - 128;
     long long s = 0;
-    int o = 0;
-    uint32_t uo = 0;                                   // operand ring slot and its use count
     for (long long k = 0; k < my_units && !abort_s; ++k) {
       int it, jt, kc, nst;
       long long kbeg;
@@ -167,12 +167,13 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
         }
         const long long kc0 = kbeg + (long long)st * (GC_KB / 2);
         const unsigned char* rs = raw + slot * RAW_BYTES;
+        const int o = (int)(s % GC_NBUF);
         if (arow) {
-          float h[32];
+          float h[32], l[32];
 #pragma unroll
           for (int q = 0; q < 8; ++q) {
             float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (kc0 + 2 * q < kend)
+            if (aact && kc0 + 2 * q < kend)
               x = *reinterpret_cast<const float4*>(rs + ar * 128 + ((q ^ (ar & 7)) << 4));
             if (aprime) x = make_float4(-x.y, x.x, -x.w, x.z);   // (-ai, ar) per complex
             h[4 * q] = x.x;
@@ -184,15 +185,18 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
 #pragma unroll
           for (int e = 0; e < 32; ++e) {
             const float hv = tf32_rn(h[e]);
-            h[e] = alo ? tf32_rn(h[e] - hv) : hv;
+            l[e] = tf32_rn(h[e] - hv);
+            h[e] = hv;
           }
-          if (!mbar_wait(&op_empty[o], (uo + 1) & 1)) {
+          if (!mbar_wait(&op_empty[o], (uint32_t)(((s / GC_NBUF) + 1) & 1))) {
             abort_s = 1;
             atomicExch(a.err, 1);
             break;
           }
           fence_after_sync();
-          tmem_st32(lane_base + COL_A + (uint32_t)(o * GC_KB), h);
+          const uint32_t col = COL_A + (uint32_t)(o * 2 * GC_KB);
+          tmem_st32(lane_base + col, h);
+          tmem_st32(lane_base + col + GC_KB, l);
           tmem_wait_st();
           fence_before_sync();
           mbar_arrive(&op_full[o]);
@@ -203,11 +207,11 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
             const int e = bt + u * 128;
             const int rb = e % NB, q = e / NB;
             v[u] = (kc0 + 2 * q < kend)
-                       ? *reinterpret_cast<const float4*>(rs + (GC_MT + rb) * 128 + ((q ^ (rb & 7)) << 4))
+                       ? *reinterpret_cast<const float4*>(rs + (a.mt + rb) * 128 + ((q ^ (rb & 7)) << 4))
                        : make_float4(0.f, 0.f, 0.f, 0.f);
           }
           mbar_arrive(&raw_empty[slot]);
-          if (!mbar_wait(&op_empty[o], (uo + 1) & 1)) {
+          if (!mbar_wait(&op_empty[o], (uint32_t)(((s / GC_NBUF) + 1) & 1))) {
             abort_s = 1;
             atomicExch(a.err, 1);
             break;
@@ -227,19 +231,12 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
           fence_async_smem();
           mbar_arrive(&op_full[o]);
         }
-        if (++o == NBUF) {
-          o = 0;
-          ++uo;
-        }
       }
     }
   } else if (warp < 12) {
     // ---------------- drain ----------------
-    // lane L: A row (L & 31), Re (A) or Im (A') by bit 5, hi lanes (< 64) add hh + hl,
-    // lo lanes add lh; each half writes its own partial slot
     const int lq = warp & 3;
-    const int L = lq * 32 + lane;
-    const bool lo_lane = L >= 64, im = (L & 32) != 0;
+    const int L = lq * 32 + lane;                       // TMEM lane = M row
     const uint32_t lane_base = tmem + ((uint32_t)(lq * 32) << 16);
     float acc[NB];
 #pragma unroll
@@ -264,20 +261,21 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
           float d1[8], d2[8];
           tmem_ld8x2(ta + c0, ta + NB + c0, d1, d2);
 #pragma unroll
-          for (int t = 0; t < 8; ++t) acc[c0 + t] += lo_lane ? d1[t] : d1[t] + d2[t];
+          for (int t = 0; t < 8; ++t) acc[c0 + t] += d1[t] + d2[t];
         }
         fence_before_sync();
         mbar_arrive(&acc_empty[ab]);
       }
       if (abort_s) break;
-      const int i = it * GC_MT + (L & 31);
-      if (i < a.ma) {
-        double* dst = a.partial + (((long long)i * a.mb) * (2 * a.nk) + 2 * kc + (lo_lane ? 1 : 0)) * 2 +
-                      (im ? 1 : 0);
+      // unit partial: lanes [0, mt) Re of A rows, [mt, 2mt) Im
+      const bool re = L < a.mt, im = L >= a.mt && L < 2 * a.mt;
+      const int i = it * a.mt + (re ? L : L - a.mt);
+      if ((re || im) && i < a.ma) {
 #pragma unroll
         for (int c = 0; c < NB; ++c) {
           const int j = jt * NB + c;
-          if (j < a.mb) dst[(long long)j * (2 * a.nk) * 2] = (double)acc[c];
+          if (j < a.mb)
+            a.partial[(((long long)i * a.mb + j) * a.nk + kc) * 2 + (re ? 0 : 1)] = (double)acc[c];
         }
       }
 #pragma unroll
@@ -285,17 +283,15 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
     }
   } else if (warp == GC_MMA_WARP && lane == 0) {
     // ---------------- MMA issue ----------------
-    const uint32_t idesc = idesc_tf32(128, 2 * NB);
+    const uint32_t id1 = idesc_tf32(128, 2 * NB), id2 = idesc_tf32(128, NB);
     const uint64_t bdesc0 = gram_desc(smem_u32(bst));
-    long long q = 0;
-    int o = 0;
-    uint32_t uo = 0;
+    long long s = 0, q = 0;
     bool issued = false;
     for (long long k = 0; k < my_units && !abort_s; ++k) {
       int it, jt, kc, nst;
       long long kbeg;
       unit_of(k, it, jt, kc, kbeg, nst);
-      for (int st = 0; st < nst; ++st) {
+      for (int st = 0; st < nst; ++st, ++s) {
         const bool seg_first = (st % GC_SEG) == 0;
         const bool seg_last = (st % GC_SEG) == GC_SEG - 1 || st == nst - 1;
         const int ab = (int)(q & 1);
@@ -304,25 +300,25 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
           atomicExch(a.err, 1);
           break;
         }
-        if (!mbar_wait(&op_full[o], uo & 1)) {
+        const int o = (int)(s % GC_NBUF);
+        if (!mbar_wait(&op_full[o], (uint32_t)((s / GC_NBUF) & 1))) {
           abort_s = 1;
           atomicExch(a.err, 1);
           break;
         }
         fence_after_sync();
         const uint32_t d = tmem + (uint32_t)(ab * 2 * NB);
-        const uint32_t at = tmem + COL_A + (uint32_t)(o * GC_KB);
+        const uint32_t a_hi = tmem + COL_A + (uint32_t)(o * 2 * GC_KB), a_lo = a_hi + GC_KB;
         // descriptors differ from the base one only in the start-address field
         const uint64_t bB = bdesc0 + (uint64_t)((o * B_BYTES) >> 4);
 #pragma unroll
-        for (int g = 0; g < GC_KB / 8; ++g)
-          mma_tf32_ts(d, at + 8 * g, bB + (uint64_t)(g * 256 >> 4), idesc, (seg_first && g == 0) ? 0u : 1u);
+        for (int g = 0; g < GC_KB / 8; ++g) {
+          const uint64_t off = (uint64_t)(g * 256 >> 4);
+          mma_tf32_ts(d, a_hi + 8 * g, bB + off, id1, (seg_first && g == 0) ? 0u : 1u);
+          mma_tf32_ts(d + NB, a_lo + 8 * g, bB + off, id2, 1u);
+        }
         mma_commit(&op_empty[o]);
         issued = true;
-        if (++o == NBUF) {
-          o = 0;
-          ++uo;
-        }
         if (seg_last) {
           mma_commit(&acc_full[ab]);
           ++q;
@@ -342,7 +338,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
       int it, jt, kc, nst;
       long long kbeg;
       unit_of(k, it, jt, kc, kbeg, nst);
-      const int i0 = it * GC_MT, j0 = jt * NB;
+      const int i0 = it * a.mt, j0 = jt * NB;
       for (int st = 0; st < nst; ++st, ++s) {
         const int slot = (int)(s % GC_RAW);
         if (!mbar_wait(&raw_empty[slot], (uint32_t)(((s / GC_RAW) + 1) & 1))) {
@@ -352,9 +348,9 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
         }
         const long long kc0 = kbeg + (long long)st * (GC_KB / 2);
         unsigned char* dst = raw + slot * RAW_BYTES;
-        mbar_arrive_expect_tx(&raw_full[slot], (uint32_t)RAW_BYTES);
+        mbar_arrive_expect_tx(&raw_full[slot], (uint32_t)((a.mt + NB) * 128));
         tma_load_2d(dst, &map_a, (int)(2 * kc0), i0, &raw_full[slot]);
-        tma_load_2d(dst + GC_MT * 128, &map_b, (int)(2 * kc0), j0, &raw_full[slot]);
+        tma_load_2d(dst + a.mt * 128, &map_b, (int)(2 * kc0), j0, &raw_full[slot]);
         issued = s + 1;
       }
     }
@@ -368,11 +364,9 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
   if (warp == GC_MMA_WARP) tmem_dealloc(tmem, TCOLS);
 }
 
-// one warp per Gram entry over its contiguous partials (2 per K-chunk), fixed shuffle
-// tree; `conj_t` writes the conjugate transpose (the operands were swapped)
-__global__ void tc_gram_reduce_kernel(const double2* __restrict__ partial, int nsplit, int ma, int mb,
-                                      int conj_t, double2* __restrict__ G) {
-  const int n = ma * mb;
+// one warp per Gram entry over its contiguous unit partials, fixed shuffle tree
+__global__ void tc_gram_reduce_kernel(const double2* __restrict__ partial, int nsplit, int n,
+                                      double2* __restrict__ G) {
   const int e = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (e >= n) return;
@@ -387,21 +381,14 @@ __global__ void tc_gram_reduce_kernel(const double2* __restrict__ partial, int n
     sr += __shfl_xor_sync(0xffffffffu, sr, o);
     si += __shfl_xor_sync(0xffffffffu, si, o);
   }
-  if (lane == 0) {
-    if (conj_t) {
-      const int i = e / mb, j = e - i * mb;
-      G[(long long)j * ma + i] = make_double2(sr, -si);
-    } else {
-      G[e] = make_double2(sr, si);
-    }
-  }
+  if (lane == 0) G[e] = make_double2(sr, si);
 }
 
-int tc_nb(int mb) { return mb <= 16 ? 16 : (mb <= 32 ? 32 : (mb <= 64 ? 64 : 96)); }
+int tc_nb(int mb) { return mb <= 16 ? 16 : (mb <= 32 ? 32 : 64); }
 
 template <int NB>
 size_t gc_smem() {
-  const size_t s = (size_t)gc_nbuf<NB>() * 2 * NB * GC_KB * 4 + (size_t)GC_RAW * (GC_MT + NB) * 128 + 1024;
+  const size_t s = (size_t)gc_nbuf<NB>() * 2 * NB * GC_KB * 4 + (size_t)GC_RAW * (64 + NB) * 128 + 1024;
   return s < (size_t)GC_SMEM_MIN ? (size_t)GC_SMEM_MIN : s;
 }
 
@@ -419,15 +406,15 @@ int sm_count_dev() {
 }
 
 struct GcPlan {
-  int nb, nit, njt, nk;
+  int mt, nb, nit, njt, nk;
   long long kchunk;
 };
 
-// ma, mb as the kernel sees them (the smaller matrix on the A side)
 GcPlan gc_plan(int ma, int mb, long long K) {
   GcPlan p;
+  p.mt = ma <= 32 ? 32 : 64;
   p.nb = tc_nb(mb);
-  p.nit = (ma + GC_MT - 1) / GC_MT;
+  p.nit = (ma + p.mt - 1) / p.mt;
   p.njt = (mb + p.nb - 1) / p.nb;
   const long long tiles = (long long)p.nit * p.njt;
   const long long sms = sm_count_dev();
@@ -444,7 +431,7 @@ GcPlan gc_plan(int ma, int mb, long long K) {
 
 template <int NB>
 int launch_gc(const GcPlan& p, cudaStream_t st, const float* A, const float* B, int ma, int mb,
-              long long K, double* part, int* err) {
+               long long K, double* part, int* err) {
   GcArgs a;
   a.partial = part;
   a.err = err;
@@ -452,11 +439,12 @@ int launch_gc(const GcPlan& p, cudaStream_t st, const float* A, const float* B, 
   a.kchunk = p.kchunk;
   a.ma = ma;
   a.mb = mb;
+  a.mt = p.mt;
   a.nit = p.nit;
   a.njt = p.njt;
   a.nk = p.nk;
   CUtensorMap ma_map, mb_map;
-  if (!ef::make_tmap_2d(&ma_map, A, ma, 2 * K, GC_KB, GC_MT, true) ||
+  if (!ef::make_tmap_2d(&ma_map, A, ma, 2 * K, GC_KB, p.mt, true) ||
       !ef::make_tmap_2d(&mb_map, B, mb, 2 * K, GC_KB, NB, true))
     return ef_fail(EF_ERR_CUDA, "gram_tc: tensor map encoding failed");
   const size_t smem = gc_smem<NB>();
@@ -472,8 +460,8 @@ int launch_gc(const GcPlan& p, cudaStream_t st, const float* A, const float* B, 
 
 extern "C" size_t ef_gram_tc_workspace_bytes(int ma, int mb, long long K) {
   if (ma <= 0 || mb <= 0 || K <= 0) return 0;
-  const GcPlan p = ma <= mb ? gc_plan(ma, mb, K) : gc_plan(mb, ma, K);
-  return (size_t)2 * p.nk * ma * mb * 2 * sizeof(double) + 512;
+  const GcPlan p = gc_plan(ma, mb, K);
+  return (size_t)p.nk * ma * mb * 2 * sizeof(double) + 512;
 }
 
 extern "C" int ef_gram_tc(const float* A, const float* B, int ma, int mb, long long K, double* G,
@@ -485,22 +473,14 @@ extern "C" int ef_gram_tc(const float* A, const float* B, int ma, int mb, long l
   if (!work || work_bytes < ef_gram_tc_workspace_bytes(ma, mb, K))
     return ef_fail(EF_ERR_WORKSPACE, "gram_tc work buffer too small");
   cudaStream_t st = (cudaStream_t)stream;
-  // the smaller matrix goes on the A side (its 32-row tiles are re-read per B tile);
-  // G = (B^H A)^H when the operands are swapped
-  const bool swap = ma > mb;
-  const float* X = swap ? B : A;
-  const float* Y = swap ? A : B;
-  const int mx = swap ? mb : ma, my = swap ? ma : mb;
-  const GcPlan p = gc_plan(mx, my, K);
+  const GcPlan p = gc_plan(ma, mb, K);
   ef_count_launches(2);
   int rc;
-  if (p.nb == 16) rc = launch_gc<16>(p, st, X, Y, mx, my, K, (double*)work, err_dev);
-  else if (p.nb == 32) rc = launch_gc<32>(p, st, X, Y, mx, my, K, (double*)work, err_dev);
-  else if (p.nb == 64) rc = launch_gc<64>(p, st, X, Y, mx, my, K, (double*)work, err_dev);
-  else rc = launch_gc<96>(p, st, X, Y, mx, my, K, (double*)work, err_dev);
+  if (p.nb == 16) rc = launch_gc<16>(p, st, A, B, ma, mb, K, (double*)work, err_dev);
+  else if (p.nb == 32) rc = launch_gc<32>(p, st, A, B, ma, mb, K, (double*)work, err_dev);
+  else rc = launch_gc<64>(p, st, A, B, ma, mb, K, (double*)work, err_dev);
   if (rc != EF_OK) return rc;
-  const int n = mx * my;
-  tc_gram_reduce_kernel<<<(n + 7) / 8, 256, 0, st>>>((const double2*)work, 2 * p.nk, mx, my, swap ? 1 : 0,
-                                                     (double2*)G);
+  const int n = ma * mb;
+  tc_gram_reduce_kernel<<<(n + 7) / 8, 256, 0, st>>>((const double2*)work, p.nk, n, (double2*)G);
   return ef_check_launch();
 }

@@ -302,3 +302,21 @@ def test_gram_tensor_core_matches_fp64(gpu, ma, mb, K):
     ref = A.astype(np.complex128).conj() @ B.astype(np.complex128).T
     assert int(err.item()) == 0
     assert np.abs(got.cpu().numpy() - ref).max() < 5e-6 * np.abs(ref).max()
+
+
+def test_gram_tensor_core_many_units_per_cta(gpu):
+    """Large K: every CTA of the persistent kernel walks several K-chunk units, and two
+    calls give identical results (no pipeline race)."""
+    from eigenfns_gb300 import blas
+    K = 2 ** 21
+    g = torch.Generator(device="cuda").manual_seed(7)
+    A = torch.randn((32, K), dtype=torch.complex64, device="cuda", generator=g)
+    B = torch.randn((48, K), dtype=torch.complex64, device="cuda", generator=g)
+    g1, e1 = blas.gram_tc(A, B)
+    g2, e2 = blas.gram_tc(A, B)
+    assert int(e1.item()) == 0 and int(e2.item()) == 0
+    assert torch.equal(g1, g2)
+    ref = (A.cpu().numpy().astype(np.complex128).conj() @ B.cpu().numpy().astype(np.complex128).T)
+    assert np.abs(g1.cpu().numpy() - ref).max() < 5e-6 * np.abs(ref).max()
+    r1 = blas.rotate(np.eye(32, dtype=np.complex64), A)
+    assert torch.equal(r1, blas.rotate(np.eye(32, dtype=np.complex64), A))
