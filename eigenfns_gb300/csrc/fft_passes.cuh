@@ -29,6 +29,14 @@ namespace ef {
 
 constexpr int kThreads = 256;
 
+// tile-size caps (tuning knobs; the defaults are the tuned values)
+#ifndef EF_NZ_CAP
+#define EF_NZ_CAP 32          // y/x passes: z-columns per tile
+#endif
+#ifndef EF_NRZ_ITEMS
+#define EF_NRZ_ITEMS 256      // z passes: work items per tile
+#endif
+
 template <int R1_, int R2_>
 struct Geo {
   static constexpr int R1 = R1_, R2 = R2_, G = R1_ * R2_;
@@ -46,15 +54,15 @@ struct Geo {
   // step, pass E (R1 >= R2) runs NRE*R1 in its second; both stay within 256 items
   // and 64 KB of exchange buffer
   static constexpr int nrz_pick(int per_row) {
-    int c = 256 / per_row > 0 ? 256 / per_row : 1;
+    int c = EF_NRZ_ITEMS / per_row > 0 ? EF_NRZ_ITEMS / per_row : 1;
     while (c > 1 && (((G * G) % c) != 0 || 3 * c * PS * 8 > 64 * 1024)) --c;
     return c;
   }
   static constexpr int NRA = nrz_pick(R2_);
   static constexpr int NRE = nrz_pick(R1_);
-  // y/x-pass z-columns per tile: largest divisor of G not above 32
+  // y/x-pass z-columns per tile: largest divisor of G not above EF_NZ_CAP
   static constexpr int nz_pick() {
-    int c = G < 32 ? G : 32;
+    int c = G < EF_NZ_CAP ? G : EF_NZ_CAP;
     while (c > 1 && (G % c != 0 || 2 * c * PS * 8 > 80 * 1024)) --c;
     return c;
   }
