@@ -14,9 +14,12 @@ tables are on the device before the timed region; vector blocks are ~1 GB, far
 larger than L2). `e2e` repeats the solve through the public API from host
 memory: the eps grid is copied from pinned host memory and the operator built
 inside the timed region, and the eigenvalues and eigenvectors are copied back to
-pinned host memory. `roofline` reports the fused Θ pipeline (5 pass kernels per
-application): algorithmic bytes = 32 B per voxel per vector + 4 B per voxel of
-eps^-1 per call, over the CUDA-event time of each call measured on its stream.
+pinned host memory. The fused Θ pipeline (5 pass kernels per
+application) is reported in `theta_roofline` (HBM on algorithmic bytes = 32 B per
+voxel per vector + 4 B per voxel of eps^-1 per call, FP32 on its flops); `roofline`
+itself is the kernel family with the largest share of the timed region (the
+Gram at this workload), achieved = its algorithmic bytes over the CUDA-event time
+of each call measured on its stream.
 `cpu_baseline` times the numpy/scipy oracle (all host cores) on a bounded
 sample of the same solve (block setup plus one LOBPCG iteration) and
 extrapolates to the whole solve with the GPU run's iteration count.
@@ -57,11 +60,16 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def _traffic_profile():
-    p = ROOT / "profiles" / "theta_traffic.json"
-    if p.exists():
-        return json.loads(p.read_text())
-    return None
+# DRAM traffic over algorithmic bytes from single-kernel ncu captures (profiles/):
+# tc_gram_96x96_K512k.md (1.21 GB read + 0.01 GB written for 0.805 GB algorithmic),
+# tc_rotate_96x64_K512k.md (0.403 + 0.223 GB for 0.671 GB), theta_passes_128.md
+# (340 MB per vector for 71 MB algorithmic)
+TRAFFIC_RATIO = {"gram": 1.52, "rotate": 0.93, "theta": 4.8}
+# FP32 flops of one Θ application per voxel and vector: 6 complex 3-D FFTs
+# (5 N log2 N each) plus the curl, frame and multiply work (~40 per voxel)
+def _theta_flops_per_voxel(G: int) -> float:
+    import math
+    return 6 * 5 * 3 * math.log2(G) + 40
 
 
 class ClockSampler:
@@ -164,7 +172,8 @@ def run_reference(args, w):
     from eigenfns_gb300.structure import generate_network
     from oracle.structure import rasterize_averaged
     # the same seeded structure, rasterized by the numpy checker (no library code on this arm)
-    net = generate_network(w["nodes"], w["seed"] + rank)
+    from eigenfns_gb300.replicas import replica_seed
+    net = generate_network(w["nodes"], replica_seed(w["seed"], rank))
     eps, L = rasterize_averaged(net.rods, w["grid"], net.box_size, sub=w["sub"]), net.box_size
     prof = _solve_profile()
     vals = []
@@ -186,14 +195,20 @@ def run_reference(args, w):
     return 0
 
 
+# The GPU solve of this workload takes 394 LOBPCG iterations in 9 blocks (measured on
+# a GB300; the oracle's per-iteration cost is extrapolated with these counts when the
+# reference arm runs alone)
+GPU_SOLVE_PROFILE = {"iterations": 394, "blocks": 9}
+
+
 def _solve_profile():
-    p = ROOT / "profiles" / "c2_solve_profile.json"
-    return json.loads(p.read_text()) if p.exists() else {}
+    return dict(GPU_SOLVE_PROFILE)
 
 
 def _structure(w, rank):
     from eigenfns_gb300.structure import make_structure
-    eps, L, _ = make_structure(w["nodes"], w["grid"], seed=w["seed"] + rank, sub=w["sub"])
+    from eigenfns_gb300.replicas import replica_seed
+    eps, L, _ = make_structure(w["nodes"], w["grid"], seed=replica_seed(w["seed"], rank), sub=w["sub"])
     return eps, L
 
 
@@ -316,15 +331,8 @@ def run_ours(args, w):
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_s = starts[0].elapsed_time(ends[-1]) / 1e3
     modes = sum(len(v) for v in vals_list)
-    tsum = torch.tensor([total_s, float(modes)], dtype=torch.float64, device=dev)
-    if world > 1:
-        tmax = tsum.clone()
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        dist.all_reduce(tsum, op=dist.ReduceOp.SUM)
-        total_all = float(tmax[0])
-        modes_all = float(tsum[1])
-    else:
-        total_all, modes_all = total_s, float(modes)
+    from eigenfns_gb300.replicas import aggregate
+    total_all, modes_all = aggregate(total_s, modes, dev)
     value = modes_all / total_all
 
     # roofline of the kernel with the largest share of the timed region
@@ -334,10 +342,20 @@ def run_ours(args, w):
     th = ops[dom]
     achieved = th["bytes"] / (th["total_ms"] * 1e-3) / 1e9
     peak, peak_kind = _peaks()
-    prof = _traffic_profile()
-    traffic = None
-    if prof and prof.get("grid") == G and prof.get("kernel") == dom:
-        traffic = prof["bytes_per_call"]
+    alg_per_call = th["bytes"] / max(th["calls"], 1)
+    traffic = alg_per_call * TRAFFIC_RATIO[dom] if dom in TRAFFIC_RATIO else None
+    # the fused Θ pipeline against both roofs (HBM on algorithmic bytes, FP32 on flops)
+    theta_roof = None
+    if "theta" in ops:
+        tq = ops["theta"]
+        gbs = tq["bytes"] / (tq["total_ms"] * 1e-3) / 1e9
+        vecs_per_s = tq["bytes"] / (32.0 * G ** 3 + 4.0 * G ** 3 / max(w["block"], 1)) / (tq["total_ms"] * 1e-3)
+        tflops = vecs_per_s * _theta_flops_per_voxel(G) * G ** 3 / 1e12
+        fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12       # FMA lanes x 2 flops x max SM clock
+        theta_roof = {"achieved_GBs": gbs, "hbm_frac": gbs / peak, "achieved_TFLOPs": tflops,
+                      "fp32_peak_TFLOPs": fp32_peak, "fp32_frac": tflops / fp32_peak,
+                      "us_per_vector": 1e6 / vecs_per_s,
+                      "traffic_per_vector": TRAFFIC_RATIO["theta"] * 32.0 * G ** 3}
 
     # e2e through the public API with host buffers (pinned), same solve
     e2e = None
@@ -420,7 +438,10 @@ def run_ours(args, w):
                      "frac": achieved / peak, "traffic": traffic, "kernel": dom,
                      "peak_source": peak_kind,
                      "mean_ms_per_call": th["mean_ms_per_call"],
-                     "algorithmic_bytes_per_call": th["bytes"] / max(th["calls"], 1)},
+                     "algorithmic_bytes_per_call": alg_per_call,
+                     "traffic_source": "ncu DRAM bytes / algorithmic bytes of the same kernel on a "
+                                       "smaller case (profiles/), scaled to this call's bytes"},
+        "theta_roofline": theta_roof,
         "kernels": {k: {"share_of_step": v["total_ms"] / sum(step_ms), "calls": v["calls"],
                         "mean_ms": v["mean_ms_per_call"], "GB/s": v["gbs"], "TFLOP/s": v["tflops"]}
                     for k, v in ops.items()},

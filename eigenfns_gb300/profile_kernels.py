@@ -6,6 +6,7 @@
     python -m eigenfns_gb300.profile_kernels rotate --ma 96 --mb 64 --grid 128
     python -m eigenfns_gb300.profile_kernels cheb --grid 192 --m 8 --steps 8
     python -m eigenfns_gb300.profile_kernels kpm --grid 256 --m 4 --steps 8
+    python -m eigenfns_gb300.profile_kernels rowstats --ma 32 --mb 32 --grid 128
 
 Each runs 3 warm-up calls and then one timed call (CUDA events on the current
 stream), printing the time; under ncu, skip the warm-up launches with -s.
@@ -40,7 +41,8 @@ def _timed(fn, warm: int = 3) -> float:
 
 def main(argv=None) -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("kernel", choices=["theta", "precond", "gram", "gram_tc", "rotate", "cheb", "kpm"])
+    ap.add_argument("kernel", choices=["theta", "precond", "gram", "gram_tc", "rotate", "cheb", "kpm",
+                                       "rowstats", "residual"])
     ap.add_argument("--grid", type=int, default=128)
     ap.add_argument("--m", type=int, default=2)
     ap.add_argument("--ma", type=int, default=32)
@@ -70,7 +72,13 @@ def main(argv=None) -> None:
         K = 2 * G ** 3
         A = torch.randn((a.ma, K), dtype=torch.complex64, device="cuda", generator=g)
         B = torch.randn((a.mb, K), dtype=torch.complex64, device="cuda", generator=g)
-        if a.kernel == "gram":
+        if a.kernel == "rowstats":
+            ms = _timed(lambda: blas.rowstats(A, B[: a.ma]))
+        elif a.kernel == "residual":
+            lam = torch.rand(a.ma, dtype=torch.float64, device="cuda")
+            R = torch.empty_like(A)
+            ms = _timed(lambda: blas.residual_norms(B[: a.ma], A, lam, R))
+        elif a.kernel == "gram":
             ms = _timed(lambda: blas.gram(A, B))
         elif a.kernel == "gram_tc":
             ms = _timed(lambda: blas.gram_tc(A, B))
