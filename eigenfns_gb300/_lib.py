@@ -54,6 +54,8 @@ SIGNATURES = {
     "ef_gram_noalloc": (_i, [_vp, _vp, _i, _i, _ll, _vp, _vp]),
     "ef_gram_tc_workspace_bytes": (_sz, [_i, _i, _ll]),
     "ef_tc_error": (_i, [_vp]),
+    "ef_energy_workspace_bytes": (_i, [_vp, _i]),
+    "ef_energy_density": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _sz, _vp]),
     "ef_gram_tc": (_i, [_vp, _vp, _i, _i, _ll, _vp, _vp, _vp, _sz, _vp]),
     "ef_rotate": (_i, [_vp, _vp, _vp, _i, _i, _ll, _i, _vp]),
     "ef_rowdot_workspace_bytes": (_sz, [_i, _ll]),

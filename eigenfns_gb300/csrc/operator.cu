@@ -218,6 +218,65 @@ int run_pipe(const ef_op* op, const Pipe& pp, const float2* X, float2* out, floa
 
 }  // namespace
 
+// ---- field outputs: energy density and participation sums ------------------------
+// u(r) = eps(r) * sum_c |E_c(r)|^2 per mode (run_modes.py:119-124) and the sums
+// (sum u, sum u^2) in fp64 behind the participation ratio PR = (sum u)^2 / sum u^2
+// (localization.py:23-29). One CTA row per mode; block partials reduced in fp64.
+constexpr int kEnergyBlocks = 152;
+
+__global__ void __launch_bounds__(256) energy_kernel(const float2* __restrict__ E, const float* __restrict__ eps,
+                                                     long long N, float* __restrict__ u,
+                                                     double* __restrict__ partial) {
+  const int v = blockIdx.y;
+  const float2* e0 = E + (long long)v * 3 * N;
+  double s1 = 0.0, s2 = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < N;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float2 a = e0[i], b = e0[N + i], c = e0[2 * N + i];
+    const float val = eps[i] * (a.x * a.x + a.y * a.y + b.x * b.x + b.y * b.y + c.x * c.x + c.y * c.y);
+    if (u) u[(long long)v * N + i] = val;
+    s1 += (double)val;
+    s2 += (double)val * (double)val;
+  }
+  __shared__ double r1[8], r2[8];
+  for (int o = 16; o > 0; o >>= 1) {
+    s1 += __shfl_down_sync(0xffffffffu, s1, o);
+    s2 += __shfl_down_sync(0xffffffffu, s2, o);
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) {
+    r1[w] = s1;
+    r2[w] = s2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t1 = 0.0, t2 = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      t1 += r1[k];
+      t2 += r2[k];
+    }
+    partial[((long long)v * gridDim.x + blockIdx.x) * 2] = t1;
+    partial[((long long)v * gridDim.x + blockIdx.x) * 2 + 1] = t2;
+  }
+}
+
+__global__ void energy_reduce_kernel(const double* __restrict__ partial, double* __restrict__ sums) {
+  const int v = blockIdx.x, lane = threadIdx.x;
+  double t1 = 0.0, t2 = 0.0;
+  for (int b = lane; b < kEnergyBlocks; b += 32) {
+    t1 += partial[((long long)v * kEnergyBlocks + b) * 2];
+    t2 += partial[((long long)v * kEnergyBlocks + b) * 2 + 1];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    t1 += __shfl_down_sync(0xffffffffu, t1, o);
+    t2 += __shfl_down_sync(0xffffffffu, t2, o);
+  }
+  if (lane == 0) {
+    sums[2 * v] = t1;
+    sums[2 * v + 1] = t2;
+  }
+}
+
 extern "C" {
 
 int ef_supported_grid(int grid) { return find_plan(grid) != nullptr; }
@@ -398,6 +457,24 @@ int ef_e_realspace(const ef_op* op, const float* X, const float* vec_scale_dev, 
                    void* stream) {
   if (!vec_scale_dev) return ef_fail(EF_ERR_INVALID, "null vec_scale");
   return realspace(op, X, Eout, vec_scale_dev, m, BUILD_THETA, W_INV_ONLY_EPS, (cudaStream_t)stream);
+}
+
+int ef_energy_workspace_bytes(const ef_op* op, int m) {
+  if (!op || m <= 0) return 0;
+  return (int)((size_t)m * kEnergyBlocks * 2 * sizeof(double) + 256);
+}
+
+int ef_energy_density(const ef_op* op, const float* E, float* u, double* sums, int m, void* work,
+                      size_t work_bytes, void* stream) {
+  if (!op || !E || !sums || m <= 0) return ef_fail(EF_ERR_INVALID, "bad energy_density arguments");
+  if (!work || work_bytes < (size_t)ef_energy_workspace_bytes(op, m))
+    return ef_fail(EF_ERR_WORKSPACE, "energy_density work buffer too small");
+  cudaStream_t st = (cudaStream_t)stream;
+  ef_count_launches(2);
+  energy_kernel<<<dim3(kEnergyBlocks, m), 256, 0, st>>>((const float2*)E, op->eps_raw, op->N, u,
+                                                         (double*)work);
+  energy_reduce_kernel<<<m, 32, 0, st>>>((const double*)work, sums);
+  return ef_check_launch();
 }
 
 int ef_cheb_first(const ef_op* op, const float* T0, float* T1, float* Y, int m, double s, float c0,

@@ -89,6 +89,14 @@ int ef_h_realspace(const ef_op* op, const float* X, float* H, int m, void* strea
 int ef_e_realspace(const ef_op* op, const float* X, const float* vec_scale_dev, float* Eout,
                    int m, void* stream);
 
+/* energy density u = eps * sum_c |E_c|^2 of real-space E fields (m,3,G,G,G) complex64
+ * (run_modes.py:119-124) into u (m,G,G,G) float32 (may be NULL), and per mode the fp64
+ * sums (sum u, sum u^2) into sums (m,2) device doubles, from which the participation
+ * ratio PR = (sum u)^2 / sum u^2 follows (localization.py:23-29) */
+int ef_energy_workspace_bytes(const ef_op* op, int m);
+int ef_energy_density(const ef_op* op, const float* E, float* u, double* sums, int m, void* work,
+                      size_t work_bytes, void* stream);
+
 /* ---- fused Chebyshev / KPM recurrences ------------------------------------------ */
 /* Bandpass filter Y = sum_k c_k T_k(B) X with B = s*Θ - 1, s = 2/lambda_max
  * (_apply_cheb_poly, interior.py:336-354).

@@ -320,3 +320,29 @@ def test_gram_tensor_core_many_units_per_cta(gpu):
     assert np.abs(g1.cpu().numpy() - ref).max() < 5e-6 * np.abs(ref).max()
     r1 = blas.rotate(np.eye(32, dtype=np.complex64), A)
     assert torch.equal(r1, blas.rotate(np.eye(32, dtype=np.complex64), A))
+
+
+def test_energy_density_and_participation_match_oracle(gpu):
+    """u = eps |E|^2 (run_modes.py:119-124) and PR = (sum u)^2 / sum u^2
+    (localization.py:23-29) against the complex128 oracle."""
+    from eigenfns_gb300.localization import energy_density, mode_participation, participation
+    from eigenfns_gb300.operator import MaxwellOperator
+    from eigenfns_gb300.structure import make_structure
+    from oracle.localization import energy_density as ref_u, participation as ref_pr
+    from oracle.operator import MaxwellOperator as Ref
+    eps, L, _ = make_structure(64, 16, seed=4)
+    k = (0.1, -0.2, 0.05)
+    op = MaxwellOperator(eps, L, k_frac=k)
+    ref = Ref(eps, L, k_frac=k, dtype=np.complex128)
+    rng = np.random.default_rng(2)
+    H = (rng.standard_normal((5, 2, 16, 16, 16)) + 1j * rng.standard_normal((5, 2, 16, 16, 16))).astype(np.complex64)
+    vals = np.array([3.0, 4.0, 5.5, 7.0, 9.0])
+    u, sums = energy_density(op, H, vals, chunk=2)
+    uref = ref_u(ref, H.astype(np.complex128), vals)
+    assert np.abs(u.cpu().numpy() - uref).max() < 2e-5 * np.abs(uref).max()
+    prs = mode_participation(op, H, vals, chunk=3)
+    for i in range(5):
+        want = ref_pr(uref[i])
+        assert prs[i]["pr_vox"] == pytest.approx(want["pr_vox"], rel=1e-4)
+        assert participation(u[i])["pr_fraction"] == pytest.approx(want["pr_fraction"], rel=1e-4)
+        assert sums[i, 0] == pytest.approx(uref[i].sum(), rel=1e-4)

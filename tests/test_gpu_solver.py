@@ -151,3 +151,34 @@ def test_rasterizer_matches_oracle(gpu):
     ref = rasterize_averaged(net.rods, 16, net.box_size, sub=3)
     assert np.array_equal(eps, ref)
     assert 1.0 <= eps.min() and eps.max() <= 8.41 + 1e-6
+
+
+def test_chebsi_bottom_up_matches_dense(golden, gpu):
+    """Bottom-up ChebSI (chebyshev.py:103-210): lowest bands equal the dense spectrum."""
+    from eigenfns_gb300.chebyshev import chebsi_bottom_up
+    from oracle.dense import dense_spectrum
+    from oracle.operator import MaxwellOperator as Ref
+    op = op_from(golden, "op8")
+    vals, vecs, st = chebsi_bottom_up(op, 8, guard=8, degree=60, tol=1e-5, max_outer=40, verbose=False)
+    w = dense_spectrum(Ref(golden["op8_eps"], 1.0, dtype=np.complex128))[2:2 + 8]
+    assert vals.shape == (8,)
+    assert np.abs(vals - w).max() / w.max() < 1e-5
+    assert st.theta_applications > 0
+
+
+def test_lobpcg_resumable_checkpoint_and_resume(golden, gpu, tmp_path):
+    """Blocks are checkpointed as they lock; a resumed run continues from them and
+    reproduces the uninterrupted eigenvalues (solver.py:385-411, io.py:31-67)."""
+    from eigenfns_gb300.io import BlockCheckpointer
+    from eigenfns_gb300.solver import lobpcg_blocks, lobpcg_blocks_resumable
+    op = op_from(golden, "op8")
+    full, _, _ = lobpcg_blocks(op, 12, m=8, guard=3, tol=1e-6, maxit=300, verbose=False)
+    ck = BlockCheckpointer(tmp_path, "solve")
+    part, _, _ = lobpcg_blocks_resumable(op, 5, m=8, guard=3, tol=1e-6, maxit=300, verbose=False,
+                                         checkpointer=ck)
+    assert (tmp_path / "solve_block000_vals.npy").exists()
+    res, vecs, _ = lobpcg_blocks_resumable(op, 12, m=8, guard=3, tol=1e-6, maxit=300, verbose=False,
+                                           checkpointer=ck, resume=True)
+    assert np.allclose(res[:5], part, rtol=1e-6)
+    assert np.abs(res - full).max() / full.max() < 1e-5
+    assert vecs.shape[0] == 12

@@ -162,3 +162,14 @@ def test_bloch_k_reduces_to_shifted_planewaves():
     KX, KY, KZ = np.meshgrid(k1 + k0[0], k1 + k0[1], k1 + k0[2], indexing="ij")
     ana = np.sort(np.concatenate([(KX ** 2 + KY ** 2 + KZ ** 2).ravel() / eps0] * 2))
     assert (np.abs(w - ana) / np.maximum(ana, 1e-12)).max() < 5e-6
+
+
+def test_oracle_participation_limits():
+    """PR of a uniform density is N_vox (fraction 1); of a single voxel 1."""
+    from oracle.localization import participation
+    u = np.ones((4, 4, 4))
+    assert participation(u)["pr_vox"] == pytest.approx(64.0)
+    assert participation(u)["pr_fraction"] == pytest.approx(1.0)
+    v = np.zeros((4, 4, 4))
+    v[1, 2, 3] = 5.0
+    assert participation(v)["pr_vox"] == pytest.approx(1.0)
