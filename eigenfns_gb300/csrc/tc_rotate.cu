@@ -8,14 +8,14 @@
 // gives the complex result. Three TF32 products per pair (x = hi + lo) give
 // fp32-class accuracy: D += A_hi B_hi + A_hi B_lo + A_lo B_hi.
 // The accumulate modes out (+/-)= ... fold the current output into the same GEMM:
-// its m_out rows are appended to S (from the next 16-row boundary) with identity
+// its m_out rows are appended to S (from the next 32-row boundary) with identity
 // coefficients and C is negated for subtraction, so every mode ends in a plain store.
 //
 // Tiles are 128 real positions (M = 128 TMEM lanes); N = 2 * m_out padded to 8.
 // A persistent CTA (448 threads) walks its tiles with four warp roles:
-//   warp 13     loads: one 2-D TMA box (16 rows x 128 positions, 8 KB, zero fill
+//   warp 13     loads: one 2-D TMA box (32 rows x 128 positions, 16 KB, zero fill
 //               outside the matrix) per stage into a raw shared-memory ring;
-//   warps 0-7   convert: each thread owns one position (= one TMEM lane) and 8 rows
+//   warps 0-7   convert: each thread owns one position (= one TMEM lane) and 16 rows
 //               of the stage, splits hi/lo and writes them with tcgen05.st into a
 //               ring of TMEM operand stages (the MMA's A operand lives in TMEM);
 //   warp 12     one thread issues the MMAs of each stage (A from TMEM, the resident
@@ -47,10 +47,11 @@ constexpr int TR_EPI0 = 256;              // first epilogue thread (warps 8-11)
 constexpr int TR_MMA_WARP = 12;
 constexpr int TR_LOAD_WARP = 13;
 constexpr int TR_M = 128;                 // real positions per tile
-constexpr int TR_JC = 16;                 // rows of S per stage
+constexpr int TR_JC = 32;                 // rows of S per stage
+constexpr int TR_RPT = TR_JC / 2;         // rows per converter thread (two warps per lane quarter)
 constexpr int TR_NBUF_MAX = 8;            // TMEM operand stages (hi + lo: 2*TR_JC columns each)
-constexpr int TR_RAW = 12;                // raw shared-memory stages
-constexpr int TR_RAW_BYTES = TR_JC * TR_M * 4;     // 8 KB per raw stage (row-major box)
+constexpr int TR_RAW = 6;                 // raw shared-memory stages
+constexpr int TR_RAW_BYTES = TR_JC * TR_M * 4;     // 16 KB per raw stage (row-major box)
 constexpr int TR_SMEM_MAX = 227 * 1024 - 1024;   // dynamic part; static barriers take the rest
 constexpr int TR_SMEM_MIN = 120 * 1024;          // keeps one CTA (and its TMEM) per SM
 
@@ -136,7 +137,7 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_c
   if (warp < 8) {
     // ---------------- converters ----------------
     // warp w writes TMEM lane quarter w % 4; thread = position p = lane of its quarter;
-    // warps 0-3 take rows 0-7 of a stage, warps 4-7 rows 8-15
+    // warps 0-3 take rows [0, TR_RPT) of a stage, warps 4-7 rows [TR_RPT, TR_JC)
     const int q4 = warp & 3, hv = warp >> 2;
     const int p = q4 * 32 + lane;
     const uint32_t lane_base = tmem + ((uint32_t)(q4 * 32) << 16);
@@ -151,10 +152,10 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_c
         break;
       }
       const float* rs = reinterpret_cast<const float*>(raw + slot * TR_RAW_BYTES) + p;
-      float hi[8], lo[8];
+      float hi[TR_RPT], lo[TR_RPT];
 #pragma unroll
-      for (int r = 0; r < 8; ++r) {
-        const float x = rs[(hv * 8 + r) * TR_M];
+      for (int r = 0; r < TR_RPT; ++r) {
+        const float x = rs[(hv * TR_RPT + r) * TR_M];
         hi[r] = tf32_rn(x);
         lo[r] = tf32_rn(x - hi[r]);
       }
@@ -165,9 +166,12 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_c
         break;
       }
       fence_after_sync();
-      const uint32_t col = col_a + (uint32_t)(o * 2 * TR_JC + hv * 8);
-      tmem_st8(lane_base + col, hi);
-      tmem_st8(lane_base + col + TR_JC, lo);
+      const uint32_t col = col_a + (uint32_t)(o * 2 * TR_JC + hv * TR_RPT);
+#pragma unroll
+      for (int r8 = 0; r8 < TR_RPT; r8 += 8) {
+        tmem_st8(lane_base + col + r8, *reinterpret_cast<const float(*)[8]>(hi + r8));
+        tmem_st8(lane_base + col + TR_JC + r8, *reinterpret_cast<const float(*)[8]>(lo + r8));
+      }
       tmem_wait_st();
       fence_before_sync();
       mbar_arrive(&op_full[o]);
