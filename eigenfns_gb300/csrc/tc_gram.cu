@@ -16,8 +16,8 @@
 // and units (K-chunks) are reduced in fp64.
 //
 // A persistent CTA (448 threads) walks work units (A-tile, B-tile, K-chunk):
-//   warp 13      loads: per 16-complex stage one 2-D TMA box of the unit's A rows and
-//                one of its B rows (128-byte swizzle, zero fill outside) into a raw
+//   warp 13      loads: per 32-complex stage two 2-D TMA boxes (128-byte swizzle, zero
+//                fill outside) of the unit's A rows and two of its B rows into a raw
 //                shared-memory ring;
 //   warps 0-3    A rows: one TMEM lane (an A or A' row) per thread, hi/lo split and
 //                tcgen05.st into a ring of TMEM operand stages (the MMA's A operand
@@ -48,9 +48,10 @@ constexpr int GC_THREADS = 448;
 constexpr int GC_CONV = 256;          // converter threads: warps 0-3 A rows, 4-7 B rows
 constexpr int GC_MMA_WARP = 12;
 constexpr int GC_LOAD_WARP = 13;
-constexpr int GC_KB = 32;             // reals per stage (16 complex) = 4 k-steps of 8
-constexpr int GC_RAW = 8;             // raw box stages
-constexpr int GC_SEG = 8;             // stages per TMEM accumulation segment
+constexpr int GC_KB = 64;             // reals per stage (32 complex) = 8 k-steps of 8
+constexpr int GC_BOX = 32;            // reals per TMA box row (128 bytes, the swizzle width)
+constexpr int GC_RAW = 4;             // raw box stages
+constexpr int GC_SEG = 4;             // stages per TMEM accumulation segment (32 k-steps)
 constexpr int GC_SMEM_MIN = 120 * 1024;   // keeps one CTA (and its TMEM) per SM
 
 // byte offset of (row r, k-quad q) in a K-major operand tile: core matrices of 8 rows
@@ -74,7 +75,7 @@ struct GcArgs {
 // operand stages (TMEM A, shared B): what TMEM holds after the two accumulators
 template <int NB>
 __host__ __device__ constexpr int gc_nbuf() {
-  return (512 - 4 * NB) / (2 * GC_KB) > 6 ? 6 : (512 - 4 * NB) / (2 * GC_KB);
+  return (512 - 4 * NB) / (2 * GC_KB) > 4 ? 4 : (512 - 4 * NB) / (2 * GC_KB);
 }
 
 // 14 warps: at most 4 per SM sub-partition, so 128 registers a thread fit
@@ -83,7 +84,8 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
                                                 const __grid_constant__ CUtensorMap map_b) {
   constexpr int GC_NBUF = gc_nbuf<NB>();
   constexpr int B_BYTES = 2 * NB * GC_KB * 4;                  // [B_hi; B_lo] per stage
-  constexpr int RAW_BYTES = (64 + NB) * 128;                   // A box + B box, 128-B rows
+  // raw stage: A boxes for reals [0,32) and [32,64) (64 rows each), then the two B boxes
+  constexpr int RAW_BYTES = (128 + 2 * NB) * 128;
   constexpr int IPB = NB * (GC_KB / 4) / 128;                  // B items per B-converter thread
   constexpr uint32_t COL_A = 4 * NB;                           // first TMEM operand column
   constexpr uint32_t TCOLS = tmem_cols_for(4 * NB + GC_NBUF * 2 * GC_KB);
@@ -140,7 +142,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
   if (warp < 8) {
     // ---------------- converters ----------------
     // warps 0-3: TMEM lane L = 32*warp + lane is A row L (L < mt) or A' row L - mt
-    // (mt <= L < 2mt); its 32 reals of the stage come from the swizzled A box.
+    // (mt <= L < 2mt); its 64 reals of the stage come from the two swizzled A boxes.
     // warps 4-7: B item e -> row e % NB, quad e / NB (consecutive threads, consecutive
     // rows: conflict-free swizzled reads and operand stores).
     // Quads past the unit's end read zero (boxes past the matrix are zero-filled).
@@ -169,25 +171,6 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
         const unsigned char* rs = raw + slot * RAW_BYTES;
         const int o = (int)(s % GC_NBUF);
         if (arow) {
-          float h[32], l[32];
-#pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (aact && kc0 + 2 * q < kend)
-              x = *reinterpret_cast<const float4*>(rs + ar * 128 + ((q ^ (ar & 7)) << 4));
-            if (aprime) x = make_float4(-x.y, x.x, -x.w, x.z);   // (-ai, ar) per complex
-            h[4 * q] = x.x;
-            h[4 * q + 1] = x.y;
-            h[4 * q + 2] = x.z;
-            h[4 * q + 3] = x.w;
-          }
-          mbar_arrive(&raw_empty[slot]);
-#pragma unroll
-          for (int e = 0; e < 32; ++e) {
-            const float hv = tf32_rn(h[e]);
-            l[e] = tf32_rn(h[e] - hv);
-            h[e] = hv;
-          }
           if (!mbar_wait(&op_empty[o], (uint32_t)(((s / GC_NBUF) + 1) & 1))) {
             abort_s = 1;
             atomicExch(a.err, 1);
@@ -195,39 +178,55 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
           }
           fence_after_sync();
           const uint32_t col = COL_A + (uint32_t)(o * 2 * GC_KB);
-          tmem_st32(lane_base + col, h);
-          tmem_st32(lane_base + col + GC_KB, l);
+#pragma unroll
+          for (int hf = 0; hf < 2; ++hf) {
+            float h[32], l[32];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+              if (aact && kc0 + 2 * (8 * hf + q) < kend)
+                x = *reinterpret_cast<const float4*>(rs + hf * 64 * 128 + ar * 128 + ((q ^ (ar & 7)) << 4));
+              if (aprime) x = make_float4(-x.y, x.x, -x.w, x.z);   // (-ai, ar) per complex
+              h[4 * q] = x.x;
+              h[4 * q + 1] = x.y;
+              h[4 * q + 2] = x.z;
+              h[4 * q + 3] = x.w;
+            }
+            if (hf == 1) mbar_arrive(&raw_empty[slot]);
+#pragma unroll
+            for (int e = 0; e < 32; ++e) {
+              const float hv = tf32_rn(h[e]);
+              l[e] = tf32_rn(h[e] - hv);
+              h[e] = hv;
+            }
+            tmem_st32(lane_base + col + hf * GC_BOX, h);
+            tmem_st32(lane_base + col + GC_KB + hf * GC_BOX, l);
+          }
           tmem_wait_st();
           fence_before_sync();
           mbar_arrive(&op_full[o]);
         } else {
-          float4 v[IPB];
-#pragma unroll
-          for (int u = 0; u < IPB; ++u) {
-            const int e = bt + u * 128;
-            const int rb = e % NB, q = e / NB;
-            v[u] = (kc0 + 2 * q < kend)
-                       ? *reinterpret_cast<const float4*>(rs + (a.mt + rb) * 128 + ((q ^ (rb & 7)) << 4))
-                       : make_float4(0.f, 0.f, 0.f, 0.f);
-          }
-          mbar_arrive(&raw_empty[slot]);
           if (!mbar_wait(&op_empty[o], (uint32_t)(((s / GC_NBUF) + 1) & 1))) {
             abort_s = 1;
             atomicExch(a.err, 1);
             break;
           }
           unsigned char* base = bst + o * B_BYTES;
-#pragma unroll
+#pragma unroll 4
           for (int u = 0; u < IPB; ++u) {
             const int e = bt + u * 128;
-            const int rb = e % NB, q = e / NB;
-            const float4 x = v[u];
+            const int rb = e % NB, q = e / NB, hf = q >> 3;   // quad q of 16: box hf, its quad q & 7
+            const float4 x = (kc0 + 2 * q < kend)
+                                 ? *reinterpret_cast<const float4*>(rs + (128 + hf * NB + rb) * 128 +
+                                                                    (((q & 7) ^ (rb & 7)) << 4))
+                                 : make_float4(0.f, 0.f, 0.f, 0.f);
             const float4 hh = make_float4(tf32_rn(x.x), tf32_rn(x.y), tf32_rn(x.z), tf32_rn(x.w));
             const float4 ll = make_float4(tf32_rn(x.x - hh.x), tf32_rn(x.y - hh.y), tf32_rn(x.z - hh.z),
                                           tf32_rn(x.w - hh.w));
             *reinterpret_cast<float4*>(base + quad_off(rb, q)) = hh;
             *reinterpret_cast<float4*>(base + quad_off(NB + rb, q)) = ll;
           }
+          mbar_arrive(&raw_empty[slot]);
           fence_async_smem();
           mbar_arrive(&op_full[o]);
         }
@@ -331,8 +330,8 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
     }
   } else if (warp == GC_LOAD_WARP && lane == 0) {
     // ---------------- loader ----------------
-    // per stage one 2-D box of the unit's A rows and one of its B rows (16 complex =
-    // 128 B per row), counted on raw_full in bytes
+    // per stage two 2-D boxes of the unit's A rows and two of its B rows (16 complex =
+    // 128 B per row and box), counted on raw_full in bytes
     long long s = 0, issued = 0;
     for (long long k = 0; k < my_units && !abort_s; ++k) {
       int it, jt, kc, nst;
@@ -348,9 +347,12 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
         }
         const long long kc0 = kbeg + (long long)st * (GC_KB / 2);
         unsigned char* dst = raw + slot * RAW_BYTES;
-        mbar_arrive_expect_tx(&raw_full[slot], (uint32_t)((a.mt + NB) * 128));
-        tma_load_2d(dst, &map_a, (int)(2 * kc0), i0, &raw_full[slot]);
-        tma_load_2d(dst + a.mt * 128, &map_b, (int)(2 * kc0), j0, &raw_full[slot]);
+        mbar_arrive_expect_tx(&raw_full[slot], (uint32_t)((2 * a.mt + 2 * NB) * 128));
+        for (int hf = 0; hf < 2; ++hf) {
+          const int x = (int)(2 * kc0) + hf * GC_BOX;
+          tma_load_2d(dst + hf * 64 * 128, &map_a, x, i0, &raw_full[slot]);
+          tma_load_2d(dst + (128 + hf * NB) * 128, &map_b, x, j0, &raw_full[slot]);
+        }
         issued = s + 1;
       }
     }
@@ -388,7 +390,7 @@ int tc_nb(int mb) { return mb <= 16 ? 16 : (mb <= 32 ? 32 : 64); }
 
 template <int NB>
 size_t gc_smem() {
-  const size_t s = (size_t)gc_nbuf<NB>() * 2 * NB * GC_KB * 4 + (size_t)GC_RAW * (64 + NB) * 128 + 1024;
+  const size_t s = (size_t)gc_nbuf<NB>() * 2 * NB * GC_KB * 4 + (size_t)GC_RAW * (128 + 2 * NB) * 128 + 1024;
   return s < (size_t)GC_SMEM_MIN ? (size_t)GC_SMEM_MIN : s;
 }
 
@@ -423,7 +425,7 @@ GcPlan gc_plan(int ma, int mb, long long K) {
   if (nk > maxk) nk = maxk;
   if (nk < 1) nk = 1;
   long long kchunk = (K + nk - 1) / nk;
-  kchunk = (kchunk + 15) / 16 * 16;
+  kchunk = (kchunk + GC_KB / 2 - 1) / (GC_KB / 2) * (GC_KB / 2);
   p.kchunk = kchunk;
   p.nk = (int)((K + kchunk - 1) / kchunk);
   return p;
@@ -444,8 +446,8 @@ int launch_gc(const GcPlan& p, cudaStream_t st, const float* A, const float* B, 
   a.njt = p.njt;
   a.nk = p.nk;
   CUtensorMap ma_map, mb_map;
-  if (!ef::make_tmap_2d(&ma_map, A, ma, 2 * K, GC_KB, p.mt, true) ||
-      !ef::make_tmap_2d(&mb_map, B, mb, 2 * K, GC_KB, NB, true))
+  if (!ef::make_tmap_2d(&ma_map, A, ma, 2 * K, GC_BOX, p.mt, true) ||
+      !ef::make_tmap_2d(&mb_map, B, mb, 2 * K, GC_BOX, NB, true))
     return ef_fail(EF_ERR_CUDA, "gram_tc: tensor map encoding failed");
   const size_t smem = gc_smem<NB>();
   ef::set_smem_once(tc_gram_kernel<NB>, smem);
