@@ -47,9 +47,11 @@ constexpr int TR_EPI0 = 256;              // first epilogue thread (warps 8-11)
 constexpr int TR_MMA_WARP = 12;
 constexpr int TR_LOAD_WARP = 13;
 constexpr int TR_M = 128;                 // real positions per tile
-constexpr int TR_NBUF_MAX = 8;            // TMEM operand stages (hi + lo: 2*JC columns each)
-// raw shared-memory stages for JC-row stages (16 KB boxes for JC = 32, 32 KB for 64)
-__host__ __device__ constexpr int tr_raw(int jc) { return jc == 32 ? 6 : 3; }
+constexpr int TR_JC = 32;                 // rows of S per stage
+constexpr int TR_RPT = TR_JC / 2;         // rows per converter thread (two warps per lane quarter)
+constexpr int TR_NBUF_MAX = 8;            // TMEM operand stages (hi + lo: 2*TR_JC columns each)
+constexpr int TR_RAW = 6;                 // raw shared-memory stages
+constexpr int TR_RAW_BYTES = TR_JC * TR_M * 4;     // 16 KB per raw stage (row-major box)
 constexpr int TR_SMEM_MAX = 227 * 1024 - 1024;   // dynamic part; static barriers take the rest
 constexpr int TR_SMEM_MIN = 120 * 1024;          // keeps one CTA (and its TMEM) per SM
 
@@ -64,30 +66,25 @@ struct TrArgs {
   float sign;           // -1 for subtraction
 };
 
-// 14 warps: at most 4 per SM sub-partition, so 128 registers a thread fit. JC rows of S
-// per stage (32 or 64); RAW raw stages of JC x 128 floats.
-template <int JC>
+// 14 warps: at most 4 per SM sub-partition, so 128 registers a thread fit
 __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_constant__ CUtensorMap map_s,
                                                   const __grid_constant__ CUtensorMap map_o) {
-  constexpr int RPT = JC / 2;             // rows per converter thread (two warps per lane quarter)
-  constexpr int RAW = tr_raw(JC);
-  constexpr int RAW_BYTES = JC * TR_M * 4;
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t op_full[TR_NBUF_MAX], op_empty[TR_NBUF_MAX];
   __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done_bar;
-  __shared__ __align__(8) uint64_t raw_full[RAW], raw_empty[RAW];
+  __shared__ __align__(8) uint64_t raw_full[TR_RAW], raw_empty[TR_RAW];
   __shared__ uint32_t tmem_base_s;
   __shared__ volatile int abort_s;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int N = 2 * a.mp;
-  const int kj = a.nch * JC;            // rows of the coefficient operand
+  const int kj = a.nch * TR_JC;            // rows of the coefficient operand
   const uint32_t b_half = (uint32_t)N * kj * 4;
   // TMA box destinations: align the raw ring to 1024 bytes
   unsigned char* raw = smem + ((1024u - (smem_u32(smem) & 1023u)) & 1023u);
-  unsigned char* bops = raw + RAW * RAW_BYTES;
+  unsigned char* bops = raw + TR_RAW * TR_RAW_BYTES;
   const uint32_t col_a = (uint32_t)(2 * N);                // first TMEM operand column
-  const uint32_t tcols = tmem_cols_for(2 * N + a.nbuf * 2 * JC);
+  const uint32_t tcols = tmem_cols_for(2 * N + a.nbuf * 2 * TR_JC);
 
   if (tid == 0) {
     abort_s = 0;
@@ -100,7 +97,7 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_c
       mbar_init(&acc_empty[b], 128);
     }
     mbar_init(&done_bar, 1);
-    for (int b = 0; b < RAW; ++b) {
+    for (int b = 0; b < TR_RAW; ++b) {
       mbar_init(&raw_full[b], 1);
       mbar_init(&raw_empty[b], TR_CONV);
     }
@@ -126,7 +123,7 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_c
     put(a.mp + i, j, a.sign * c.y);
   }
   if (a.nch > a.ncs)
-    for (int i = tid; i < a.m_out; i += TR_THREADS) put(i, a.ncs * JC + i, 1.f);
+    for (int i = tid; i < a.m_out; i += TR_THREADS) put(i, a.ncs * TR_JC + i, 1.f);
   fence_async_smem();
   if (warp == TR_MMA_WARP) tmem_alloc(&tmem_base_s, tcols);
   fence_before_sync();
@@ -140,25 +137,25 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_c
   if (warp < 8) {
     // ---------------- converters ----------------
     // warp w writes TMEM lane quarter w % 4; thread = position p = lane of its quarter;
-    // warps 0-3 take rows [0, RPT) of a stage, warps 4-7 rows [RPT, JC)
+    // warps 0-3 take rows [0, TR_RPT) of a stage, warps 4-7 rows [TR_RPT, TR_JC)
     const int q4 = warp & 3, hv = warp >> 2;
     const int p = q4 * 32 + lane;
     const uint32_t lane_base = tmem + ((uint32_t)(q4 * 32) << 16);
     int o = 0;
     uint32_t uo = 0;                                   // operand ring slot and its use count
     for (long long s = 0; s < nstages; ++s) {
-      const int slot = (int)(s % RAW);
+      const int slot = (int)(s % TR_RAW);
       if (abort_s) break;
-      if (!mbar_wait(&raw_full[slot], (uint32_t)((s / RAW) & 1))) {
+      if (!mbar_wait(&raw_full[slot], (uint32_t)((s / TR_RAW) & 1))) {
         abort_s = 1;
         atomicExch(&g_tc_error, 1);
         break;
       }
-      const float* rs = reinterpret_cast<const float*>(raw + slot * RAW_BYTES) + p;
-      float hi[RPT], lo[RPT];
+      const float* rs = reinterpret_cast<const float*>(raw + slot * TR_RAW_BYTES) + p;
+      float hi[TR_RPT], lo[TR_RPT];
 #pragma unroll
-      for (int r = 0; r < RPT; ++r) {
-        const float x = rs[(hv * RPT + r) * TR_M];
+      for (int r = 0; r < TR_RPT; ++r) {
+        const float x = rs[(hv * TR_RPT + r) * TR_M];
         hi[r] = tf32_rn(x);
         lo[r] = tf32_rn(x - hi[r]);
       }
@@ -169,11 +166,11 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_c
         break;
       }
       fence_after_sync();
-      const uint32_t col = col_a + (uint32_t)(o * 2 * JC + hv * RPT);
+      const uint32_t col = col_a + (uint32_t)(o * 2 * TR_JC + hv * TR_RPT);
 #pragma unroll
-      for (int r8 = 0; r8 < RPT; r8 += 8) {
+      for (int r8 = 0; r8 < TR_RPT; r8 += 8) {
         tmem_st8(lane_base + col + r8, *reinterpret_cast<const float(*)[8]>(hi + r8));
-        tmem_st8(lane_base + col + JC + r8, *reinterpret_cast<const float(*)[8]>(lo + r8));
+        tmem_st8(lane_base + col + TR_JC + r8, *reinterpret_cast<const float(*)[8]>(lo + r8));
       }
       tmem_wait_st();
       fence_before_sync();
@@ -237,11 +234,11 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_c
           break;
         }
         fence_after_sync();
-        const uint32_t a_hi = tmem + col_a + (uint32_t)(o * 2 * JC), a_lo = a_hi + JC;
+        const uint32_t a_hi = tmem + col_a + (uint32_t)(o * 2 * TR_JC), a_lo = a_hi + TR_JC;
         // descriptors differ from the base one only in the start-address field
-        const uint64_t bh0 = b_desc0 + (uint64_t)((c * (JC / 4) * 128) >> 4);
+        const uint64_t bh0 = b_desc0 + (uint64_t)((c * (TR_JC / 4) * 128) >> 4);
 #pragma unroll
-        for (int g = 0; g < JC / 8; ++g) {
+        for (int g = 0; g < TR_JC / 8; ++g) {
           const uint64_t bh = bh0 + (uint64_t)(g * 256 >> 4), bl = bh + (uint64_t)(b_half >> 4);
           mma_tf32_ts(d, a_hi + 8 * g, bh, idesc, (c | g) ? 1u : 0u);
           mma_tf32_ts(d, a_hi + 8 * g, bl, idesc, 1u);
@@ -271,17 +268,17 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_c
     int c = 0;
     long long issued = 0;
     for (long long s = 0; s < nstages; ++s) {
-      const int slot = (int)(s % RAW);
+      const int slot = (int)(s % TR_RAW);
       if (abort_s) break;
-      if (!mbar_wait(&raw_empty[slot], (uint32_t)(((s / RAW) + 1) & 1))) {
+      if (!mbar_wait(&raw_empty[slot], (uint32_t)(((s / TR_RAW) + 1) & 1))) {
         abort_s = 1;
         atomicExch(&g_tc_error, 1);
         break;
       }
-      mbar_arrive_expect_tx(&raw_full[slot], RAW_BYTES);
+      mbar_arrive_expect_tx(&raw_full[slot], TR_RAW_BYTES);
       const int x = (int)(tile * TR_M);
-      if (c < a.ncs) tma_load_2d(raw + slot * RAW_BYTES, &map_s, x, c * JC, &raw_full[slot]);
-      else tma_load_2d(raw + slot * RAW_BYTES, &map_o, x, (c - a.ncs) * JC, &raw_full[slot]);
+      if (c < a.ncs) tma_load_2d(raw + slot * TR_RAW_BYTES, &map_s, x, c * TR_JC, &raw_full[slot]);
+      else tma_load_2d(raw + slot * TR_RAW_BYTES, &map_o, x, (c - a.ncs) * TR_JC, &raw_full[slot]);
       issued = s + 1;
       if (++c == a.nch) {
         c = 0;
@@ -289,8 +286,8 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_c
       }
     }
     // no copy may still be landing when the CTA exits: wait for the last issued phases
-    for (long long s = issued - RAW > 0 ? issued - RAW : 0; s < issued; ++s)
-      mbar_wait(&raw_full[(int)(s % RAW)], (uint32_t)((s / RAW) & 1));
+    for (long long s = issued - TR_RAW > 0 ? issued - TR_RAW : 0; s < issued; ++s)
+      mbar_wait(&raw_full[(int)(s % TR_RAW)], (uint32_t)((s / TR_RAW) & 1));
   }
   fence_before_sync();
   __syncthreads();
@@ -311,13 +308,13 @@ int sm_count() {
   return cached[dev];
 }
 
-size_t tr_smem(int jc, int nch, int mp) {
-  const size_t s = (size_t)tr_raw(jc) * jc * TR_M * 4 + (size_t)2 * (2 * mp) * (nch * jc) * 4 + 1024;
+size_t tr_smem(int nch, int mp) {
+  const size_t s = (size_t)TR_RAW * TR_RAW_BYTES + (size_t)2 * (2 * mp) * (nch * TR_JC) * 4 + 1024;
   return s < (size_t)TR_SMEM_MIN ? (size_t)TR_SMEM_MIN : s;
 }
 
-int chunks_for(int jc, int m_in, int m_out, int mode) {
-  return (m_in + jc - 1) / jc + (mode != 0 ? (m_out + jc - 1) / jc : 0);
+int chunks_for(int m_in, int m_out, int mode) {
+  return (m_in + TR_JC - 1) / TR_JC + (mode != 0 ? (m_out + TR_JC - 1) / TR_JC : 0);
 }
 
 }  // namespace
@@ -330,32 +327,12 @@ int tc_rotate_max_rows(int m_out, int mode) {
   if (m_out <= 0 || m_out > 64) return 0;
   const int mp = (m_out + 7) / 8 * 8;
   int rows = 0;
-  while (tr_smem(32, chunks_for(32, rows + 32, m_out, mode), mp) <= (size_t)TR_SMEM_MAX) rows += 32;
+  while (tr_smem(chunks_for(rows + TR_JC, m_out, mode), mp) <= (size_t)TR_SMEM_MAX) rows += TR_JC;
   return rows;
 }
 
-template <int JC>
-int launch_rotate(TrArgs a, const float* S, float* out, int mode, cudaStream_t st) {
-  a.ncs = (a.m_in + JC - 1) / JC;
-  a.nch = chunks_for(JC, a.m_in, a.m_out, mode);
-  a.nbuf = (512 - 2 * 2 * a.mp) / (2 * JC);             // TMEM left after the accumulators
-  if (a.nbuf > TR_NBUF_MAX) a.nbuf = TR_NBUF_MAX;
-  CUtensorMap ms, mo;
-  if (!make_tmap_2d(&ms, S, a.m_in, a.n2, TR_M, JC, false) ||
-      !make_tmap_2d(&mo, out, a.m_out, a.n2, TR_M, JC, false))
-    return ef_fail(EF_ERR_CUDA, "rotate: tensor map encoding failed");
-  const size_t smem = tr_smem(JC, a.nch, a.mp);
-  ef::set_smem_once(tc_rotate_kernel<JC>, smem);
-  long long grid = sm_count();
-  if (grid > a.ntiles) grid = a.ntiles;
-  ef_count_launches(1);
-  tc_rotate_kernel<JC><<<(unsigned)grid, TR_THREADS, smem, st>>>(a, ms, mo);
-  return ef_check_launch();
-}
-
 // one pass: m_out <= 64, m_in <= tc_rotate_max_rows(m_out, mode); S and out 16-byte
-// aligned, K even. Stages of 64 rows when the outputs leave TMEM for at least three
-// of them and the shared-memory budget holds, else 32.
+// aligned, K even
 int tc_rotate_launch(const float* C, int ldc, const float* S, float* out, int m_in, int m_out,
                      long long K, int mode, cudaStream_t st) {
   TrArgs a;
@@ -367,9 +344,22 @@ int tc_rotate_launch(const float* C, int ldc, const float* S, float* out, int m_
   a.m_in = m_in;
   a.m_out = m_out;
   a.mp = (m_out + 7) / 8 * 8;
+  a.ncs = (m_in + TR_JC - 1) / TR_JC;
+  a.nch = chunks_for(m_in, m_out, mode);
   a.sign = mode < 0 ? -1.f : 1.f;
-  const bool big = a.mp <= 32 && tr_smem(64, chunks_for(64, m_in, m_out, mode), a.mp) <= (size_t)TR_SMEM_MAX;
-  return big ? launch_rotate<64>(a, S, out, mode, st) : launch_rotate<32>(a, S, out, mode, st);
+  a.nbuf = (512 - 2 * 2 * a.mp) / (2 * TR_JC);          // TMEM left after the accumulators
+  if (a.nbuf > TR_NBUF_MAX) a.nbuf = TR_NBUF_MAX;
+  CUtensorMap ms, mo;
+  if (!make_tmap_2d(&ms, S, m_in, a.n2, TR_M, TR_JC, false) ||
+      !make_tmap_2d(&mo, out, m_out, a.n2, TR_M, TR_JC, false))
+    return ef_fail(EF_ERR_CUDA, "rotate: tensor map encoding failed");
+  const size_t smem = tr_smem(a.nch, a.mp);
+  ef::set_smem_once(tc_rotate_kernel, smem);
+  long long grid = sm_count();
+  if (grid > a.ntiles) grid = a.ntiles;
+  ef_count_launches(1);
+  tc_rotate_kernel<<<(unsigned)grid, TR_THREADS, smem, st>>>(a, ms, mo);
+  return ef_check_launch();
 }
 
 // device address of the tensor-core kernels' error flag (current device)

@@ -108,6 +108,26 @@ def _normalize_rows(X: torch.Tensor, floor: float) -> None:
     blas.scale_rows(X, 1.0 / torch.clamp(torch.sqrt(torch.clamp(st[:, 2], min=0.0)), min=floor))
 
 
+def _rr_gram(act: torch.Tensor, hact: torch.Tensor, m: int) -> torch.Tensor:
+    """Rayleigh-Ritz matrix act^H (Θ act) of the active basis (m-row blocks).
+
+    Θ is Hermitian, so only the block upper triangle is computed (block row i against
+    the image blocks i..end, reading 2/3 of the rows a full Gram reads at three blocks)
+    and the lower triangle is its conjugate transpose; the caller symmetrises the
+    diagonal blocks as the reference does (solver.py:281-301).
+    """
+    nb = int(act.shape[0])
+    if nb % m or nb // m < 2:
+        return gram(act, hact)
+    A = torch.empty((nb, nb), dtype=torch.complex128, device=act.device)
+    for i in range(0, nb, m):
+        blk = gram(act[i:i + m], hact[i:])
+        A[i:i + m, i:] = blk
+        if i + m < nb:
+            A[i + m:, i:i + m] = blk[:, m:].conj().T
+    return A
+
+
 def _ritz_residuals(X, HX, R, normalize: bool):
     """(lam, relres, |x|) for the rows of X, with R = HX - lam X written into `R`.
 
@@ -216,7 +236,7 @@ def lobpcg_blocks(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
             else:
                 act, hact, off = S[m:3 * m], HS[m:3 * m], m
             nb = int(act.shape[0])
-            A_d = gram(act, hact)
+            A_d = _rr_gram(act, hact, m)
             rows_d = blas.rowstats(act, act)[:, 2]
             A = A_d.cpu().numpy()
             rownorm = np.sqrt(np.maximum(rows_d.cpu().numpy(), 0))
