@@ -690,10 +690,11 @@ int noalloc_scratch(void** out) {
 }
 }  // namespace
 
-// ef_gram runs on the tensor cores (ef_gram_tc) for Grams larger than 32 x 32 (measured
-// faster there: 64x32 1.14 vs 1.49 ms, 96x96 4.6 vs 6.5 ms at K = 4.2M) and on the CUDA
-// cores for the small ones (32x32 0.79 vs 1.14 ms); EF_GRAM_KERNEL=tc|simt overrides
-inline bool gram_use_tc(int ma, int mb) { return (long long)ma * mb > 32 * 32; }
+// ef_gram runs on the tensor cores (ef_gram_tc) from 16 x 32 up (measured at K = 4.2M:
+// 16x32 0.59 vs 0.78 ms, 32x32 0.60 vs 0.79, 64x32 0.92 vs 1.49, 96x96 4.5 vs 6.5) and
+// on the CUDA cores below, where the tensor-core kernel's fixed cost per K-stage
+// dominates; EF_GRAM_KERNEL=tc|simt overrides
+inline bool gram_use_tc(int ma, int mb) { return (long long)ma * mb >= 16 * 32; }
 
 namespace ef {
 int* tc_error_dev();

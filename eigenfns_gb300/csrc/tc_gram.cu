@@ -9,20 +9,27 @@
 // [B_hi; B_lo]. Per 8-real k-step two MMAs give fp32-class products (x = hi + lo):
 //   D[:, 0:2NB]  += A_hi [B_hi; B_lo]^T      (hh | hl)
 //   D[:, NB:2NB] += A_lo B_hi^T              (hl + lh)
+// A tiles of up to 32 rows pack two K-ranges into the 128 lanes (PK = 2): lanes [0, 64)
+// take the stage's reals [0, 32) and lanes [64, 128) its reals [32, 64) at the same
+// k-step; B is laid out as [B1_lo; B1_hi; B2_hi; B2_lo] (1, 2: the two K-ranges), so
+//   D[:, 0:4NB]  += A_hi [B1_lo; B1_hi; B2_hi; B2_lo]^T
+//   D[:, NB:3NB] += A_lo [B1_hi; B2_hi]^T
+// leaves each lane half's three products in its own 2NB columns (the other half's
+// columns hold cross terms that are never read): half the MMAs per stage.
 // Tensor-core fp32 accumulation is not round-to-nearest over long chains, so the
-// accumulation is cut into segments of SEG stages, alternating between two TMEM
-// accumulators; each finished segment is read back (tcgen05.ld) and added into fp32
-// registers while the next segment's MMAs run; a work unit's sum goes out in fp64
-// and units (K-chunks) are reduced in fp64.
+// accumulation is cut into segments of 32 k-steps, alternating between two TMEM
+// accumulators where TMEM holds two; each finished segment is read back (tcgen05.ld)
+// and added into fp32 registers while the next segment's MMAs run; a work unit's sum
+// goes out in fp64 and units (K-chunks, and the two K-ranges) are reduced in fp64.
 //
 // A persistent CTA (448 threads) walks work units (A-tile, B-tile, K-chunk):
 //   warp 13      loads: per 32-complex stage two 2-D TMA boxes (128-byte swizzle, zero
 //                fill outside) of the unit's A rows and two of its B rows into a raw
-//                shared-memory ring;
-//   warps 0-3    A rows: one TMEM lane (an A or A' row) per thread, hi/lo split and
-//                tcgen05.st into a ring of TMEM operand stages (the MMA's A operand
-//                lives in TMEM);
-//   warps 4-7    B rows: hi/lo split into a ring of K-major shared-memory stages;
+//                shared-memory ring (the shared memory the operand ring leaves);
+//   warps 0-7    two groups of four converter warps, each taking every other stage:
+//                A rows hi/lo split and tcgen05.st into a ring of TMEM operand stages
+//                (the MMA's A operand lives in TMEM, one A or A' row per lane), B rows
+//                hi/lo split into a ring of K-major shared-memory stages;
 //   warp 12      one thread issues each stage's MMAs and commits them;
 //   warps 8-11   drain finished segments (one TMEM lane per thread, all columns)
 //                and write the unit's partial sums.
@@ -45,23 +52,26 @@ namespace {
 using namespace ef::tc;
 
 constexpr int GC_THREADS = 448;
-constexpr int GC_CONV = 256;          // converter threads: warps 0-3 A rows, 4-7 B rows
+constexpr int GC_GROUP = 128;         // converter threads per stage (warps 0-3 or 4-7)
 constexpr int GC_MMA_WARP = 12;
 constexpr int GC_LOAD_WARP = 13;
 constexpr int GC_KB = 64;             // reals per stage (32 complex) = 8 k-steps of 8
 constexpr int GC_BOX = 32;            // reals per TMA box row (128 bytes, the swizzle width)
-constexpr int GC_RAW = 4;             // raw box stages
+constexpr int GC_RAW_MAX = 12;        // raw box stages at most (the rest of shared memory)
 constexpr int GC_SEG = 4;             // stages per TMEM accumulation segment (32 k-steps)
 constexpr int GC_SMEM_MIN = 120 * 1024;   // keeps one CTA (and its TMEM) per SM
 
-// byte offset of (row r, k-quad q) in a K-major operand tile: core matrices of 8 rows
-// x 16 B, K-adjacent core matrices 128 B apart, 8-row groups (GC_KB/4)*128 = 1024 B apart
+// byte offset of (row r, k-quad q) in a K-major operand tile of QPR quads per row: core
+// matrices of 8 rows x 16 B, K-adjacent core matrices 128 B apart, 8-row groups QPR*128 B
+// apart
+template <int QPR>
 __device__ __forceinline__ int quad_off(int r, int q) {
-  return (((r >> 3) * (GC_KB / 4) + q) << 7) + ((r & 7) << 4);
+  return (((r >> 3) * QPR + q) << 7) + ((r & 7) << 4);
 }
 
+template <int QPR>
 __device__ __forceinline__ uint64_t gram_desc(uint32_t addr) {
-  return smem_desc(addr, 128, (GC_KB / 4) * 128);
+  return smem_desc(addr, 128, QPR * 128);
 }
 
 struct GcArgs {
@@ -72,23 +82,50 @@ struct GcArgs {
   int ma, mb, mt, nit, njt, nk;
 };
 
-// operand stages (TMEM A, shared B): what TMEM holds after the two accumulators
-template <int NB>
-__host__ __device__ constexpr int gc_nbuf() {
-  return (512 - 4 * NB) / (2 * GC_KB) > 4 ? 4 : (512 - 4 * NB) / (2 * GC_KB);
-}
+// TMEM budget of one configuration. PK = 1: a stage's 64 reals run through 8 k-steps,
+// one accumulator is [hh | hl] (2NB columns). PK = 2 (A tiles of 32 rows): the two
+// 32-real halves of a stage go to the lane halves [0, 64) and [64, 128) side by side,
+// 4 k-steps per stage, and the accumulator is [1lo | 1hi | 2hi | 2lo] (4NB columns).
+template <int NB, int PK>
+struct GcCfg {
+  static constexpr int KS = GC_KB / 8 / PK;                    // k-steps per stage
+  static constexpr int QPR = GC_KB / 4 / PK;                   // B quads per operand row
+  static constexpr int ACOLS = 2 * GC_KB / PK;                 // TMEM columns of one A stage (hi, lo)
+  static constexpr int DCOLS = 2 * NB * PK;                    // columns of one accumulator
+  static constexpr int NACC = 2 * DCOLS + 2 * ACOLS <= 512 ? 2 : 1;
+  static constexpr int MTMAX = 64 / PK;                        // A rows per box
+  static constexpr int B_BYTES = 2 * NB * GC_KB * 4;           // [B_hi; B_lo] per stage
+  // raw stage: A boxes for reals [0,32) and [32,64), then the two B boxes
+  static constexpr int RAW_BYTES = (2 * MTMAX + 2 * NB) * 128;
+  // operand stages: what TMEM holds after the accumulators (at most 4, and at least 4 raw
+  // stages beside them in 226 KB of shared memory); the raw ring takes the rest of the
+  // shared memory, which sets the bytes in flight from HBM
+  static constexpr int SMEM_BUDGET = 226 * 1024 - 1024;
+  static constexpr int NBUF_TMEM = (512 - NACC * DCOLS) / ACOLS < 4 ? (512 - NACC * DCOLS) / ACOLS : 4;
+  static constexpr int NBUF_SMEM = (SMEM_BUDGET - 4 * RAW_BYTES) / B_BYTES;
+  static constexpr int NBUF = NBUF_TMEM < NBUF_SMEM ? NBUF_TMEM : NBUF_SMEM;
+  static constexpr int NRAW = (SMEM_BUDGET - NBUF * B_BYTES) / RAW_BYTES < GC_RAW_MAX
+                                  ? (SMEM_BUDGET - NBUF * B_BYTES) / RAW_BYTES
+                                  : GC_RAW_MAX;
+  static_assert(NBUF >= 2 && NRAW >= 4, "operand and raw rings");
+  static constexpr int SEG = GC_SEG * PK;                      // stages per segment (32 k-steps)
+};
 
 // 14 warps: at most 4 per SM sub-partition, so 128 registers a thread fit
-template <int NB>
+template <int NB, int PK>
 __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_constant__ CUtensorMap map_a,
                                                 const __grid_constant__ CUtensorMap map_b) {
-  constexpr int GC_NBUF = gc_nbuf<NB>();
-  constexpr int B_BYTES = 2 * NB * GC_KB * 4;                  // [B_hi; B_lo] per stage
-  // raw stage: A boxes for reals [0,32) and [32,64) (64 rows each), then the two B boxes
-  constexpr int RAW_BYTES = (128 + 2 * NB) * 128;
+  using Cfg = GcCfg<NB, PK>;
+  constexpr int GC_NBUF = Cfg::NBUF;
+  constexpr int NACC = Cfg::NACC;
+  constexpr int B_BYTES = Cfg::B_BYTES;
+  constexpr int RAW_BYTES = Cfg::RAW_BYTES;
+  constexpr int GC_RAW = Cfg::NRAW;
+  constexpr int MTMAX = Cfg::MTMAX;
   constexpr int IPB = NB * (GC_KB / 4) / 128;                  // B items per B-converter thread
-  constexpr uint32_t COL_A = 4 * NB;                           // first TMEM operand column
-  constexpr uint32_t TCOLS = tmem_cols_for(4 * NB + GC_NBUF * 2 * GC_KB);
+  constexpr uint32_t COL_A = NACC * Cfg::DCOLS;                // first TMEM operand column
+  constexpr uint32_t TCOLS = tmem_cols_for(COL_A + GC_NBUF * Cfg::ACOLS);
+  static_assert(COL_A + GC_NBUF * Cfg::ACOLS <= 512, "TMEM budget");
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t op_full[GC_NBUF], op_empty[GC_NBUF];
   __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done_bar;
@@ -106,7 +143,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
   if (tid == 0) {
     abort_s = 0;
     for (int b = 0; b < GC_NBUF; ++b) {
-      mbar_init(&op_full[b], GC_CONV);
+      mbar_init(&op_full[b], GC_GROUP);
       mbar_init(&op_empty[b], 1);
     }
     for (int b = 0; b < 2; ++b) {
@@ -116,7 +153,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
     mbar_init(&done_bar, 1);
     for (int b = 0; b < GC_RAW; ++b) {
       mbar_init(&raw_full[b], 1);
-      mbar_init(&raw_empty[b], GC_CONV);
+      mbar_init(&raw_empty[b], GC_GROUP);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -141,18 +178,22 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
 
   if (warp < 8) {
     // ---------------- converters ----------------
-    // warps 0-3: TMEM lane L = 32*warp + lane is A row L (L < mt) or A' row L - mt
-    // (mt <= L < 2mt); its 64 reals of the stage come from the two swizzled A boxes.
-    // warps 4-7: B item e -> row e % NB, quad e / NB (consecutive threads, consecutive
-    // rows: conflict-free swizzled reads and operand stores).
+    // Two groups of four warps take alternate stages (group g the stages s with s % 2 == g),
+    // so one stage's waits and TMEM stores overlap the next stage's work. In a group,
+    // thread t (TMEM lane t) converts:
+    //   A rows: lane l < mt is A row l, mt <= l < 2mt is A' row l - mt; PK = 1: l = t, both
+    //   halves of the stage; PK = 2: l = t & 63, the half t >> 6 (reals [32 h, 32 h + 32));
+    //   B items e = t + 128 u -> row e % NB, quad e / NB (consecutive threads, consecutive
+    //   rows: conflict-free swizzled reads and operand stores).
     // Quads past the unit's end read zero (boxes past the matrix are zero-filled).
-    const bool arow = warp < 4;
-    const int L = warp * 32 + lane;
-    const bool aprime = arow && L >= a.mt;
-    const int ar = aprime ? L - a.mt : L;
-    const bool aact = arow && L < 2 * a.mt;
+    const int grp = warp >> 2;
+    const int t = tid & 127;
+    const int rg = PK == 2 ? (t >> 6) : 0;
+    const int l = PK == 2 ? (t & 63) : t;
+    const bool aprime = l >= a.mt;
+    const int ar = aprime ? l - a.mt : l;
+    const bool aact = l < 2 * a.mt;
     const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
-    const int bt = tid - 128;
     long long s = 0;
     for (long long k = 0; k < my_units && !abort_s; ++k) {
       int it, jt, kc, nst;
@@ -161,82 +202,79 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
       long long kend = kbeg + a.kchunk;
       if (kend > a.K) kend = a.K;
       for (int st = 0; st < nst; ++st, ++s) {
+        if ((int)(s & 1) != grp) continue;
         const int slot = (int)(s % GC_RAW);
-        if (!mbar_wait(&raw_full[slot], (uint32_t)((s / GC_RAW) & 1))) {
+        const int o = (int)(s % GC_NBUF);
+        if (!mbar_wait(&raw_full[slot], (uint32_t)((s / GC_RAW) & 1)) ||
+            !mbar_wait(&op_empty[o], (uint32_t)(((s / GC_NBUF) + 1) & 1))) {
           abort_s = 1;
           atomicExch(a.err, 1);
           break;
         }
+        fence_after_sync();
         const long long kc0 = kbeg + (long long)st * (GC_KB / 2);
         const unsigned char* rs = raw + slot * RAW_BYTES;
-        const int o = (int)(s % GC_NBUF);
-        if (arow) {
-          if (!mbar_wait(&op_empty[o], (uint32_t)(((s / GC_NBUF) + 1) & 1))) {
-            abort_s = 1;
-            atomicExch(a.err, 1);
-            break;
-          }
-          fence_after_sync();
-          const uint32_t col = COL_A + (uint32_t)(o * 2 * GC_KB);
-#pragma unroll
-          for (int hf = 0; hf < 2; ++hf) {
-            float h[32], l[32];
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-              float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
-              if (aact && kc0 + 2 * (8 * hf + q) < kend)
-                x = *reinterpret_cast<const float4*>(rs + hf * 64 * 128 + ar * 128 + ((q ^ (ar & 7)) << 4));
-              if (aprime) x = make_float4(-x.y, x.x, -x.w, x.z);   // (-ai, ar) per complex
-              h[4 * q] = x.x;
-              h[4 * q + 1] = x.y;
-              h[4 * q + 2] = x.z;
-              h[4 * q + 3] = x.w;
-            }
-            if (hf == 1) mbar_arrive(&raw_empty[slot]);
-#pragma unroll
-            for (int e = 0; e < 32; ++e) {
-              const float hv = tf32_rn(h[e]);
-              l[e] = tf32_rn(h[e] - hv);
-              h[e] = hv;
-            }
-            tmem_st32(lane_base + col + hf * GC_BOX, h);
-            tmem_st32(lane_base + col + GC_KB + hf * GC_BOX, l);
-          }
-          tmem_wait_st();
-          fence_before_sync();
-          mbar_arrive(&op_full[o]);
-        } else {
-          if (!mbar_wait(&op_empty[o], (uint32_t)(((s / GC_NBUF) + 1) & 1))) {
-            abort_s = 1;
-            atomicExch(a.err, 1);
-            break;
-          }
-          unsigned char* base = bst + o * B_BYTES;
+        // B rows -> shared-memory operand stage
+        unsigned char* base = bst + o * B_BYTES;
 #pragma unroll 4
-          for (int u = 0; u < IPB; ++u) {
-            const int e = bt + u * 128;
-            const int rb = e % NB, q = e / NB, hf = q >> 3;   // quad q of 16: box hf, its quad q & 7
-            const float4 x = (kc0 + 2 * q < kend)
-                                 ? *reinterpret_cast<const float4*>(rs + (128 + hf * NB + rb) * 128 +
-                                                                    (((q & 7) ^ (rb & 7)) << 4))
-                                 : make_float4(0.f, 0.f, 0.f, 0.f);
-            const float4 hh = make_float4(tf32_rn(x.x), tf32_rn(x.y), tf32_rn(x.z), tf32_rn(x.w));
-            const float4 ll = make_float4(tf32_rn(x.x - hh.x), tf32_rn(x.y - hh.y), tf32_rn(x.z - hh.z),
-                                          tf32_rn(x.w - hh.w));
-            *reinterpret_cast<float4*>(base + quad_off(rb, q)) = hh;
-            *reinterpret_cast<float4*>(base + quad_off(NB + rb, q)) = ll;
+        for (int u = 0; u < IPB; ++u) {
+          const int e = t + u * 128;
+          const int rb = e % NB, q = e / NB, hf = q >> 3;   // quad q of 16: box hf, its quad q & 7
+          const float4 x = (kc0 + 2 * q < kend)
+                               ? *reinterpret_cast<const float4*>(rs + (2 * MTMAX + hf * NB + rb) * 128 +
+                                                                  (((q & 7) ^ (rb & 7)) << 4))
+                               : make_float4(0.f, 0.f, 0.f, 0.f);
+          const float4 hh = make_float4(tf32_rn(x.x), tf32_rn(x.y), tf32_rn(x.z), tf32_rn(x.w));
+          const float4 ll = make_float4(tf32_rn(x.x - hh.x), tf32_rn(x.y - hh.y), tf32_rn(x.z - hh.z),
+                                        tf32_rn(x.w - hh.w));
+          if (PK == 1) {
+            *reinterpret_cast<float4*>(base + quad_off<Cfg::QPR>(rb, q)) = hh;
+            *reinterpret_cast<float4*>(base + quad_off<Cfg::QPR>(NB + rb, q)) = ll;
+          } else {   // rows [1lo | 1hi | 2hi | 2lo]
+            *reinterpret_cast<float4*>(base + quad_off<Cfg::QPR>((hf ? 2 * NB : NB) + rb, q & 7)) = hh;
+            *reinterpret_cast<float4*>(base + quad_off<Cfg::QPR>((hf ? 3 * NB : 0) + rb, q & 7)) = ll;
           }
-          mbar_arrive(&raw_empty[slot]);
-          fence_async_smem();
-          mbar_arrive(&op_full[o]);
         }
+        // A rows -> TMEM operand stage
+        const uint32_t col = COL_A + (uint32_t)(o * Cfg::ACOLS);
+#pragma unroll
+        for (int h2 = 0; h2 < 2 / PK; ++h2) {
+          const int hf = PK == 2 ? rg : h2;
+          float h[32], lo[32];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (aact && kc0 + 2 * (8 * hf + q) < kend)
+              x = *reinterpret_cast<const float4*>(rs + hf * MTMAX * 128 + ar * 128 + ((q ^ (ar & 7)) << 4));
+            if (aprime) x = make_float4(-x.y, x.x, -x.w, x.z);   // (-ai, ar) per complex
+            h[4 * q] = x.x;
+            h[4 * q + 1] = x.y;
+            h[4 * q + 2] = x.z;
+            h[4 * q + 3] = x.w;
+          }
+          if (h2 == 2 / PK - 1) mbar_arrive(&raw_empty[slot]);
+#pragma unroll
+          for (int e = 0; e < 32; ++e) {
+            const float hv = tf32_rn(h[e]);
+            lo[e] = tf32_rn(h[e] - hv);
+            h[e] = hv;
+          }
+          tmem_st32(lane_base + col + h2 * GC_BOX, h);
+          tmem_st32(lane_base + col + GC_KB / PK + h2 * GC_BOX, lo);
+        }
+        tmem_wait_st();
+        fence_async_smem();
+        fence_before_sync();
+        mbar_arrive(&op_full[o]);
       }
     }
   } else if (warp < 12) {
     // ---------------- drain ----------------
     const int lq = warp & 3;
     const int L = lq * 32 + lane;                       // TMEM lane = M row
-    const uint32_t lane_base = tmem + ((uint32_t)(lq * 32) << 16);
+    const int rg = PK == 2 ? (lq >> 1) : 0;             // lane half (warp-uniform)
+    const int l = PK == 2 ? (L & 63) : L;
+    const uint32_t lane_base = tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(rg * 2 * NB);
     float acc[NB];
 #pragma unroll
     for (int c = 0; c < NB; ++c) acc[c] = 0.f;
@@ -245,16 +283,16 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
       int it, jt, kc, nst;
       long long kbeg;
       unit_of(k, it, jt, kc, kbeg, nst);
-      const int nseg = (nst + GC_SEG - 1) / GC_SEG;
+      const int nseg = (nst + Cfg::SEG - 1) / Cfg::SEG;
       for (int sg = 0; sg < nseg; ++sg, ++q) {
-        const int ab = (int)(q & 1);
-        if (!mbar_wait(&acc_full[ab], (uint32_t)((q >> 1) & 1))) {
+        const int ab = (int)(q % NACC);
+        if (!mbar_wait(&acc_full[ab], (uint32_t)((q / NACC) & 1))) {
           abort_s = 1;
           atomicExch(a.err, 1);
           break;
         }
         fence_after_sync();
-        const uint32_t ta = lane_base + (uint32_t)(ab * 2 * NB);
+        const uint32_t ta = lane_base + (uint32_t)(ab * Cfg::DCOLS);
 #pragma unroll
         for (int c0 = 0; c0 < NB; c0 += 8) {
           float d1[8], d2[8];
@@ -266,15 +304,16 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
         mbar_arrive(&acc_empty[ab]);
       }
       if (abort_s) break;
-      // unit partial: lanes [0, mt) Re of A rows, [mt, 2mt) Im
-      const bool re = L < a.mt, im = L >= a.mt && L < 2 * a.mt;
-      const int i = it * a.mt + (re ? L : L - a.mt);
+      // unit partial: lanes [0, mt) Re of A rows, [mt, 2mt) Im (of each lane half)
+      const bool re = l < a.mt, im = l >= a.mt && l < 2 * a.mt;
+      const int i = it * a.mt + (re ? l : l - a.mt);
       if ((re || im) && i < a.ma) {
 #pragma unroll
         for (int c = 0; c < NB; ++c) {
           const int j = jt * NB + c;
           if (j < a.mb)
-            a.partial[(((long long)i * a.mb + j) * a.nk + kc) * 2 + (re ? 0 : 1)] = (double)acc[c];
+            a.partial[(((long long)i * a.mb + j) * (a.nk * PK) + kc * PK + rg) * 2 + (re ? 0 : 1)] =
+                (double)acc[c];
         }
       }
 #pragma unroll
@@ -282,8 +321,10 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
     }
   } else if (warp == GC_MMA_WARP && lane == 0) {
     // ---------------- MMA issue ----------------
-    const uint32_t id1 = idesc_tf32(128, 2 * NB), id2 = idesc_tf32(128, NB);
-    const uint64_t bdesc0 = gram_desc(smem_u32(bst));
+    const uint32_t id1 = idesc_tf32(128, 2 * NB * PK), id2 = idesc_tf32(128, NB * PK);
+    const uint64_t bdesc0 = gram_desc<Cfg::QPR>(smem_u32(bst));
+    // B_hi rows, the second MMA's operand: [0, NB) for PK = 1, [NB, 3NB) for PK = 2
+    constexpr uint64_t b2off = PK == 2 ? (uint64_t)(((NB / 8) * Cfg::QPR * 128) >> 4) : 0;
     long long s = 0, q = 0;
     bool issued = false;
     for (long long k = 0; k < my_units && !abort_s; ++k) {
@@ -291,10 +332,10 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
       long long kbeg;
       unit_of(k, it, jt, kc, kbeg, nst);
       for (int st = 0; st < nst; ++st, ++s) {
-        const bool seg_first = (st % GC_SEG) == 0;
-        const bool seg_last = (st % GC_SEG) == GC_SEG - 1 || st == nst - 1;
-        const int ab = (int)(q & 1);
-        if (seg_first && !mbar_wait(&acc_empty[ab], (uint32_t)(((q >> 1) + 1) & 1))) {
+        const bool seg_first = (st % Cfg::SEG) == 0;
+        const bool seg_last = (st % Cfg::SEG) == Cfg::SEG - 1 || st == nst - 1;
+        const int ab = (int)(q % NACC);
+        if (seg_first && !mbar_wait(&acc_empty[ab], (uint32_t)(((q / NACC) + 1) & 1))) {
           abort_s = 1;
           atomicExch(a.err, 1);
           break;
@@ -306,15 +347,15 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
           break;
         }
         fence_after_sync();
-        const uint32_t d = tmem + (uint32_t)(ab * 2 * NB);
-        const uint32_t a_hi = tmem + COL_A + (uint32_t)(o * 2 * GC_KB), a_lo = a_hi + GC_KB;
+        const uint32_t d = tmem + (uint32_t)(ab * Cfg::DCOLS);
+        const uint32_t a_hi = tmem + COL_A + (uint32_t)(o * Cfg::ACOLS), a_lo = a_hi + GC_KB / PK;
         // descriptors differ from the base one only in the start-address field
         const uint64_t bB = bdesc0 + (uint64_t)((o * B_BYTES) >> 4);
 #pragma unroll
-        for (int g = 0; g < GC_KB / 8; ++g) {
+        for (int g = 0; g < Cfg::KS; ++g) {
           const uint64_t off = (uint64_t)(g * 256 >> 4);
           mma_tf32_ts(d, a_hi + 8 * g, bB + off, id1, (seg_first && g == 0) ? 0u : 1u);
-          mma_tf32_ts(d + NB, a_lo + 8 * g, bB + off, id2, 1u);
+          mma_tf32_ts(d + NB, a_lo + 8 * g, bB + b2off + off, id2, 1u);
         }
         mma_commit(&op_empty[o]);
         issued = true;
@@ -350,8 +391,8 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
         mbar_arrive_expect_tx(&raw_full[slot], (uint32_t)((2 * a.mt + 2 * NB) * 128));
         for (int hf = 0; hf < 2; ++hf) {
           const int x = (int)(2 * kc0) + hf * GC_BOX;
-          tma_load_2d(dst + hf * 64 * 128, &map_a, x, i0, &raw_full[slot]);
-          tma_load_2d(dst + (128 + hf * NB) * 128, &map_b, x, j0, &raw_full[slot]);
+          tma_load_2d(dst + hf * MTMAX * 128, &map_a, x, i0, &raw_full[slot]);
+          tma_load_2d(dst + (2 * MTMAX + hf * NB) * 128, &map_b, x, j0, &raw_full[slot]);
         }
         issued = s + 1;
       }
@@ -366,9 +407,11 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
   if (warp == GC_MMA_WARP) tmem_dealloc(tmem, TCOLS);
 }
 
-// one warp per Gram entry over its contiguous unit partials, fixed shuffle tree
+// one warp per Gram entry over its contiguous unit partials, fixed shuffle tree; with
+// ld_t > 0 the computed (n / ld_t, ld_t) matrix is B^H A and entry e goes out conjugated
+// to its transposed place in G = A^H B
 __global__ void tc_gram_reduce_kernel(const double2* __restrict__ partial, int nsplit, int n,
-                                      double2* __restrict__ G) {
+                                      int ld_t, double2* __restrict__ G) {
   const int e = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (e >= n) return;
@@ -383,14 +426,18 @@ __global__ void tc_gram_reduce_kernel(const double2* __restrict__ partial, int n
     sr += __shfl_xor_sync(0xffffffffu, sr, o);
     si += __shfl_xor_sync(0xffffffffu, si, o);
   }
-  if (lane == 0) G[e] = make_double2(sr, si);
+  if (lane == 0) {
+    if (ld_t > 0) G[(long long)(e % ld_t) * (n / ld_t) + e / ld_t] = make_double2(sr, -si);
+    else G[e] = make_double2(sr, si);
+  }
 }
 
 int tc_nb(int mb) { return mb <= 16 ? 16 : (mb <= 32 ? 32 : 64); }
 
-template <int NB>
+template <int NB, int PK>
 size_t gc_smem() {
-  const size_t s = (size_t)gc_nbuf<NB>() * 2 * NB * GC_KB * 4 + (size_t)GC_RAW * (128 + 2 * NB) * 128 + 1024;
+  using Cfg = GcCfg<NB, PK>;
+  const size_t s = (size_t)Cfg::NBUF * Cfg::B_BYTES + (size_t)Cfg::NRAW * Cfg::RAW_BYTES + 1024;
   return s < (size_t)GC_SMEM_MIN ? (size_t)GC_SMEM_MIN : s;
 }
 
@@ -408,13 +455,26 @@ int sm_count_dev() {
 }
 
 struct GcPlan {
-  int mt, nb, nit, njt, nk;
+  int mt, nb, pk, nit, njt, nk;
   long long kchunk;
 };
+
+// A tiles of up to 32 rows fill the 128 TMEM lanes with both halves of a stage (pk = 2)
+// unless EF_GRAM_TC_PACK=0
+bool gc_pack_enabled() {
+  const char* e = getenv("EF_GRAM_TC_PACK");
+  return !(e && e[0] == '0');
+}
+
+// G = A^H B with more than 32 rows of A and at most 32 of B runs as (B^H A)^H: the
+// 32-row side in the packed A tiles (32x64 0.82 ms vs 64x32 0.92, 32x96 1.59 vs 96x32 1.81
+// at K = 4.2M)
+bool gc_swap(int ma, int mb) { return ma > 32 && mb <= 32 && gc_pack_enabled(); }
 
 GcPlan gc_plan(int ma, int mb, long long K) {
   GcPlan p;
   p.mt = ma <= 32 ? 32 : 64;
+  p.pk = (p.mt == 32 && gc_pack_enabled()) ? 2 : 1;
   p.nb = tc_nb(mb);
   p.nit = (ma + p.mt - 1) / p.mt;
   p.njt = (mb + p.nb - 1) / p.nb;
@@ -431,7 +491,7 @@ GcPlan gc_plan(int ma, int mb, long long K) {
   return p;
 }
 
-template <int NB>
+template <int NB, int PK>
 int launch_gc(const GcPlan& p, cudaStream_t st, const float* A, const float* B, int ma, int mb,
                long long K, double* part, int* err) {
   GcArgs a;
@@ -449,12 +509,12 @@ int launch_gc(const GcPlan& p, cudaStream_t st, const float* A, const float* B, 
   if (!ef::make_tmap_2d(&ma_map, A, ma, 2 * K, GC_BOX, p.mt, true) ||
       !ef::make_tmap_2d(&mb_map, B, mb, 2 * K, GC_BOX, NB, true))
     return ef_fail(EF_ERR_CUDA, "gram_tc: tensor map encoding failed");
-  const size_t smem = gc_smem<NB>();
-  ef::set_smem_once(tc_gram_kernel<NB>, smem);
+  const size_t smem = gc_smem<NB, PK>();
+  ef::set_smem_once(tc_gram_kernel<NB, PK>, smem);
   long long units = (long long)p.nit * p.njt * p.nk;
   long long grid = sm_count_dev();
   if (grid > units) grid = units;
-  tc_gram_kernel<NB><<<(unsigned)grid, GC_THREADS, smem, st>>>(a, ma_map, mb_map);
+  tc_gram_kernel<NB, PK><<<(unsigned)grid, GC_THREADS, smem, st>>>(a, ma_map, mb_map);
   return EF_OK;
 }
 
@@ -462,8 +522,8 @@ int launch_gc(const GcPlan& p, cudaStream_t st, const float* A, const float* B, 
 
 extern "C" size_t ef_gram_tc_workspace_bytes(int ma, int mb, long long K) {
   if (ma <= 0 || mb <= 0 || K <= 0) return 0;
-  const GcPlan p = gc_plan(ma, mb, K);
-  return (size_t)p.nk * ma * mb * 2 * sizeof(double) + 512;
+  const GcPlan p = gc_swap(ma, mb) ? gc_plan(mb, ma, K) : gc_plan(ma, mb, K);
+  return (size_t)p.nk * p.pk * ma * mb * 2 * sizeof(double) + 512;
 }
 
 extern "C" int ef_gram_tc(const float* A, const float* B, int ma, int mb, long long K, double* G,
@@ -475,14 +535,31 @@ extern "C" int ef_gram_tc(const float* A, const float* B, int ma, int mb, long l
   if (!work || work_bytes < ef_gram_tc_workspace_bytes(ma, mb, K))
     return ef_fail(EF_ERR_WORKSPACE, "gram_tc work buffer too small");
   cudaStream_t st = (cudaStream_t)stream;
+  const bool swap = gc_swap(ma, mb);
+  if (swap) {
+    const float* t = A;
+    A = B;
+    B = t;
+    const int tm = ma;
+    ma = mb;
+    mb = tm;
+  }
   const GcPlan p = gc_plan(ma, mb, K);
   ef_count_launches(2);
   int rc;
-  if (p.nb == 16) rc = launch_gc<16>(p, st, A, B, ma, mb, K, (double*)work, err_dev);
-  else if (p.nb == 32) rc = launch_gc<32>(p, st, A, B, ma, mb, K, (double*)work, err_dev);
-  else rc = launch_gc<64>(p, st, A, B, ma, mb, K, (double*)work, err_dev);
+  double* part = (double*)work;
+  if (p.pk == 2) {
+    if (p.nb == 16) rc = launch_gc<16, 2>(p, st, A, B, ma, mb, K, part, err_dev);
+    else if (p.nb == 32) rc = launch_gc<32, 2>(p, st, A, B, ma, mb, K, part, err_dev);
+    else rc = launch_gc<64, 2>(p, st, A, B, ma, mb, K, part, err_dev);
+  } else {
+    if (p.nb == 16) rc = launch_gc<16, 1>(p, st, A, B, ma, mb, K, part, err_dev);
+    else if (p.nb == 32) rc = launch_gc<32, 1>(p, st, A, B, ma, mb, K, part, err_dev);
+    else rc = launch_gc<64, 1>(p, st, A, B, ma, mb, K, part, err_dev);
+  }
   if (rc != EF_OK) return rc;
   const int n = ma * mb;
-  tc_gram_reduce_kernel<<<(n + 7) / 8, 256, 0, st>>>((const double2*)work, p.nk, n, (double2*)G);
+  tc_gram_reduce_kernel<<<(n + 7) / 8, 256, 0, st>>>((const double2*)work, p.nk * p.pk, n,
+                                                     swap ? mb : 0, (double2*)G);
   return ef_check_launch();
 }

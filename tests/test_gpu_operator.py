@@ -291,7 +291,9 @@ def test_rotate_tensor_core_matches_cuda_core(gpu, m_in, m_out, monkeypatch):
 
 
 @pytest.mark.parametrize("ma,mb,K", [(32, 32, 2 * 32 ** 3), (96, 96, 2 * 24 ** 3), (7, 45, 1002),
-                                     (200, 32, 2 * 16 ** 3), (64, 20, 2 * 20 ** 3 + 16)])
+                                     (200, 32, 2 * 16 ** 3), (64, 20, 2 * 20 ** 3 + 16),
+                                     (16, 16, 2 * 24 ** 3 + 2), (20, 100, 2 * 20 ** 3),
+                                     (32, 64, 2 * 40 ** 3 + 38)])
 def test_gram_tensor_core_matches_fp64(gpu, ma, mb, K):
     """3xTF32 tcgen05 Gram with segment drains and fp64 unit reduction: fp32-class accuracy."""
     from eigenfns_gb300 import blas
@@ -302,6 +304,27 @@ def test_gram_tensor_core_matches_fp64(gpu, ma, mb, K):
     ref = A.astype(np.complex128).conj() @ B.astype(np.complex128).T
     assert int(err.item()) == 0
     assert np.abs(got.cpu().numpy() - ref).max() < 5e-6 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("ma,mb", [(32, 32), (24, 64), (32, 96), (96, 32), (70, 17)])
+def test_gram_tensor_core_packed_matches_unpacked(gpu, monkeypatch, ma, mb):
+    """A tiles of <= 32 rows run both 32-real halves of a stage side by side in the TMEM
+    lanes (and A^H B with a 32-row B runs as (B^H A)^H); the unpacked layout
+    (EF_GRAM_TC_PACK=0) gives the same Gram to fp32 class."""
+    from eigenfns_gb300 import blas
+    K = 2 * 48 ** 3 + 6
+    g = torch.Generator(device="cuda").manual_seed(ma + mb)
+    A = torch.randn((ma, K), dtype=torch.complex64, device="cuda", generator=g)
+    B = torch.randn((mb, K), dtype=torch.complex64, device="cuda", generator=g)
+    packed, e1 = blas.gram_tc(A, B)
+    monkeypatch.setenv("EF_GRAM_TC_PACK", "0")
+    plain, e2 = blas.gram_tc(A, B)
+    monkeypatch.delenv("EF_GRAM_TC_PACK")
+    assert int(e1.item()) == 0 and int(e2.item()) == 0
+    ref = (A.cpu().numpy().astype(np.complex128).conj() @ B.cpu().numpy().astype(np.complex128).T)
+    scale = np.abs(ref).max()
+    assert np.abs(packed.cpu().numpy() - ref).max() < 5e-6 * scale
+    assert np.abs(plain.cpu().numpy() - ref).max() < 5e-6 * scale
 
 
 def test_gram_tensor_core_many_units_per_cta(gpu):
