@@ -691,9 +691,9 @@ int noalloc_scratch(void** out) {
 }  // namespace
 
 // ef_gram runs on the tensor cores (ef_gram_tc) from 16 x 32 up (measured at K = 4.2M:
-// 16x32 0.59 vs 0.78 ms, 32x32 0.60 vs 0.79, 64x32 0.92 vs 1.49, 96x96 4.5 vs 6.5) and
-// on the CUDA cores below, where the tensor-core kernel's fixed cost per K-stage
-// dominates; EF_GRAM_KERNEL=tc|simt overrides
+// 32x32 0.53 vs 0.79 ms, 64x32 0.73 vs 1.49, 96x96 3.5 vs 6.5) and on the CUDA cores
+// below, where the tensor-core kernel's fixed cost per K-stage dominates;
+// EF_GRAM_KERNEL=tc|simt overrides
 inline bool gram_use_tc(int ma, int mb) { return (long long)ma * mb >= 16 * 32; }
 
 namespace ef {

@@ -38,6 +38,16 @@ __device__ __forceinline__ float tf32_rn(float x) {
   return __uint_as_float(r);
 }
 
+// x = hi + lo for 3xTF32 products: hi is x rounded to the nearest tf32 value (ties away
+// from zero, like cvt.rna: add half of the 13 dropped mantissa bits, then clear them --
+// two integer operations), lo = x - hi is exact in fp32 (x and hi are within a factor of
+// two) and the tensor core reads its leading 19 bits, |error| <= 2^-21 |x| with no bias.
+// For finite |x| below the largest tf32 value (no rounding up into infinity).
+__device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
+  hi = __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xffffe000u);
+  lo = x - hi;
+}
+
 __device__ __forceinline__ void mbar_init(uint64_t* bar, int count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
 }
@@ -55,25 +65,33 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
+__device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(a), "r"(parity), "r"(kSuspendHintNs)
+      : "memory");
+  return ok != 0;
+}
+
 // waits for the phase of the given parity to complete; the waiting warp is suspended
-// inside try_wait rather than spinning on the issue slots. Returns false once
-// kWaitLimitNs of wall time has passed without completion.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// inside try_wait rather than spinning on the issue slots, and with sleep_ns > 0 it
+// also sleeps that long between tries (for waiters with slack, so that they leave the
+// issue slots to the warps on the critical path). The wall clock is read once per 16
+// tries. Returns false once kWaitLimitNs of wall time has passed without completion.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t sleep_ns = 0) {
   const uint32_t a = smem_u32(bar);
-  unsigned long long t0 = 0;
-  for (int it = 0;; ++it) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(a), "r"(parity), "r"(kSuspendHintNs)
-        : "memory");
-    if (ok) return true;
-    const unsigned long long now = global_ns();
-    if (it == 0) t0 = now;
-    else if (now - t0 > kWaitLimitNs) return false;
+  if (mbar_try(a, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (;;) {
+    for (int i = 0; i < 16; ++i) {
+      if (sleep_ns) __nanosleep(sleep_ns);
+      if (mbar_try(a, parity)) return true;
+    }
+    if (global_ns() - t0 > kWaitLimitNs) return false;
   }
 }
 

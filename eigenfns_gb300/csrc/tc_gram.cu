@@ -162,6 +162,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
   __syncthreads();
   fence_after_sync();
   const uint32_t tmem = tmem_base_s;
+  constexpr uint32_t nbuf = GC_NBUF;
 
   // k-th unit of this CTA -> (A-tile, B-tile, K-chunk), first complex index, stages
   auto unit_of = [&](long long k, int& it, int& jt, int& kc, long long& kbeg, int& nst) {
@@ -194,7 +195,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
     const int ar = aprime ? l - a.mt : l;
     const bool aact = l < 2 * a.mt;
     const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
-    long long s = 0;
+    uint32_t s = 0;                                     // stage counter (32-bit ring arithmetic)
     for (long long k = 0; k < my_units && !abort_s; ++k) {
       int it, jt, kc, nst;
       long long kbeg;
@@ -204,15 +205,16 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
       for (int st = 0; st < nst; ++st, ++s) {
         if ((int)(s & 1) != grp) continue;
         const int slot = (int)(s % GC_RAW);
-        const int o = (int)(s % GC_NBUF);
+        const int o = (int)(s % nbuf);
         if (!mbar_wait(&raw_full[slot], (uint32_t)((s / GC_RAW) & 1)) ||
-            !mbar_wait(&op_empty[o], (uint32_t)(((s / GC_NBUF) + 1) & 1))) {
+            !mbar_wait(&op_empty[o], (uint32_t)(((s / nbuf) + 1) & 1))) {
           abort_s = 1;
           atomicExch(a.err, 1);
           break;
         }
         fence_after_sync();
         const long long kc0 = kbeg + (long long)st * (GC_KB / 2);
+        const int rem = kend - kc0 < GC_KB ? (int)(kend - kc0) : GC_KB;   // complex left in the unit
         const unsigned char* rs = raw + slot * RAW_BYTES;
         // B rows -> shared-memory operand stage
         unsigned char* base = bst + o * B_BYTES;
@@ -220,13 +222,15 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
         for (int u = 0; u < IPB; ++u) {
           const int e = t + u * 128;
           const int rb = e % NB, q = e / NB, hf = q >> 3;   // quad q of 16: box hf, its quad q & 7
-          const float4 x = (kc0 + 2 * q < kend)
+          const float4 x = (2 * q < rem)
                                ? *reinterpret_cast<const float4*>(rs + (2 * MTMAX + hf * NB + rb) * 128 +
                                                                   (((q & 7) ^ (rb & 7)) << 4))
                                : make_float4(0.f, 0.f, 0.f, 0.f);
-          const float4 hh = make_float4(tf32_rn(x.x), tf32_rn(x.y), tf32_rn(x.z), tf32_rn(x.w));
-          const float4 ll = make_float4(tf32_rn(x.x - hh.x), tf32_rn(x.y - hh.y), tf32_rn(x.z - hh.z),
-                                        tf32_rn(x.w - hh.w));
+          float4 hh, ll;
+          split_tf32(x.x, hh.x, ll.x);
+          split_tf32(x.y, hh.y, ll.y);
+          split_tf32(x.z, hh.z, ll.z);
+          split_tf32(x.w, hh.w, ll.w);
           if (PK == 1) {
             *reinterpret_cast<float4*>(base + quad_off<Cfg::QPR>(rb, q)) = hh;
             *reinterpret_cast<float4*>(base + quad_off<Cfg::QPR>(NB + rb, q)) = ll;
@@ -237,14 +241,14 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
         }
         // A rows -> TMEM operand stage
         const uint32_t col = COL_A + (uint32_t)(o * Cfg::ACOLS);
-#pragma unroll
+#pragma unroll 1
         for (int h2 = 0; h2 < 2 / PK; ++h2) {
           const int hf = PK == 2 ? rg : h2;
           float h[32], lo[32];
 #pragma unroll
           for (int q = 0; q < 8; ++q) {
             float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (aact && kc0 + 2 * (8 * hf + q) < kend)
+            if (aact && 2 * (8 * hf + q) < rem)
               x = *reinterpret_cast<const float4*>(rs + hf * MTMAX * 128 + ar * 128 + ((q ^ (ar & 7)) << 4));
             if (aprime) x = make_float4(-x.y, x.x, -x.w, x.z);   // (-ai, ar) per complex
             h[4 * q] = x.x;
@@ -252,12 +256,9 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
             h[4 * q + 2] = x.z;
             h[4 * q + 3] = x.w;
           }
-          if (h2 == 2 / PK - 1) mbar_arrive(&raw_empty[slot]);
 #pragma unroll
           for (int e = 0; e < 32; ++e) {
-            const float hv = tf32_rn(h[e]);
-            lo[e] = tf32_rn(h[e] - hv);
-            h[e] = hv;
+            split_tf32(h[e], h[e], lo[e]);
           }
           tmem_st32(lane_base + col + h2 * GC_BOX, h);
           tmem_st32(lane_base + col + GC_KB / PK + h2 * GC_BOX, lo);
@@ -265,6 +266,10 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
         tmem_wait_st();
         fence_async_smem();
         fence_before_sync();
+        // the raw slot goes back to the loader only now: an arrive issued while shared
+        // loads from it are still in flight (their registers not yet consumed) let the
+        // next TMA box land under them
+        mbar_arrive(&raw_empty[slot]);
         mbar_arrive(&op_full[o]);
       }
     }
@@ -278,7 +283,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
     float acc[NB];
 #pragma unroll
     for (int c = 0; c < NB; ++c) acc[c] = 0.f;
-    long long q = 0;                                    // segment counter
+    uint32_t q = 0;                                     // segment counter
     for (long long k = 0; k < my_units && !abort_s; ++k) {
       int it, jt, kc, nst;
       long long kbeg;
@@ -286,7 +291,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
       const int nseg = (nst + Cfg::SEG - 1) / Cfg::SEG;
       for (int sg = 0; sg < nseg; ++sg, ++q) {
         const int ab = (int)(q % NACC);
-        if (!mbar_wait(&acc_full[ab], (uint32_t)((q / NACC) & 1))) {
+        if (!mbar_wait(&acc_full[ab], (uint32_t)((q / NACC) & 1), NACC == 2 ? 128u : 32u)) {
           abort_s = 1;
           atomicExch(a.err, 1);
           break;
@@ -325,7 +330,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
     const uint64_t bdesc0 = gram_desc<Cfg::QPR>(smem_u32(bst));
     // B_hi rows, the second MMA's operand: [0, NB) for PK = 1, [NB, 3NB) for PK = 2
     constexpr uint64_t b2off = PK == 2 ? (uint64_t)(((NB / 8) * Cfg::QPR * 128) >> 4) : 0;
-    long long s = 0, q = 0;
+    uint32_t s = 0, q = 0;
     bool issued = false;
     for (long long k = 0; k < my_units && !abort_s; ++k) {
       int it, jt, kc, nst;
@@ -340,8 +345,8 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
           atomicExch(a.err, 1);
           break;
         }
-        const int o = (int)(s % GC_NBUF);
-        if (!mbar_wait(&op_full[o], (uint32_t)((s / GC_NBUF) & 1))) {
+        const int o = (int)(s % nbuf);
+        if (!mbar_wait(&op_full[o], (uint32_t)((s / nbuf) & 1))) {
           abort_s = 1;
           atomicExch(a.err, 1);
           break;
@@ -373,7 +378,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
     // ---------------- loader ----------------
     // per stage two 2-D boxes of the unit's A rows and two of its B rows (16 complex =
     // 128 B per row and box), counted on raw_full in bytes
-    long long s = 0, issued = 0;
+    uint32_t s = 0, issued = 0;
     for (long long k = 0; k < my_units && !abort_s; ++k) {
       int it, jt, kc, nst;
       long long kbeg;
@@ -381,7 +386,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
       const int i0 = it * a.mt, j0 = jt * NB;
       for (int st = 0; st < nst; ++st, ++s) {
         const int slot = (int)(s % GC_RAW);
-        if (!mbar_wait(&raw_empty[slot], (uint32_t)(((s / GC_RAW) + 1) & 1))) {
+        if (!mbar_wait(&raw_empty[slot], (uint32_t)(((s / GC_RAW) + 1) & 1), 64u)) {
           abort_s = 1;
           atomicExch(a.err, 1);
           break;
@@ -398,7 +403,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
       }
     }
     // no copy may still be landing when the CTA exits: wait for the last issued phases
-    for (long long t = issued - GC_RAW > 0 ? issued - GC_RAW : 0; t < issued; ++t)
+    for (uint32_t t = issued > (uint32_t)GC_RAW ? issued - GC_RAW : 0; t < issued; ++t)
       mbar_wait(&raw_full[(int)(t % GC_RAW)], (uint32_t)((t / GC_RAW) & 1));
   }
   fence_before_sync();
@@ -466,9 +471,9 @@ bool gc_pack_enabled() {
   return !(e && e[0] == '0');
 }
 
-// G = A^H B with more than 32 rows of A and at most 32 of B runs as (B^H A)^H: the
-// 32-row side in the packed A tiles (32x64 0.82 ms vs 64x32 0.92, 32x96 1.59 vs 96x32 1.81
-// at K = 4.2M)
+// G = A^H B with more than 32 rows of A and at most 32 of B runs as (B^H A)^H, the
+// 32-row side in the packed A tiles (64x32 0.82 ms this way against 0.92 unpacked, 96x32
+// 1.59 against 1.81, at K = 4.2M)
 bool gc_swap(int ma, int mb) { return ma > 32 && mb <= 32 && gc_pack_enabled(); }
 
 GcPlan gc_plan(int ma, int mb, long long K) {
@@ -505,6 +510,7 @@ int launch_gc(const GcPlan& p, cudaStream_t st, const float* A, const float* B, 
   a.nit = p.nit;
   a.njt = p.njt;
   a.nk = p.nk;
+
   CUtensorMap ma_map, mb_map;
   if (!ef::make_tmap_2d(&ma_map, A, ma, 2 * K, GC_BOX, p.mt, true) ||
       !ef::make_tmap_2d(&mb_map, B, mb, 2 * K, GC_BOX, NB, true))

@@ -156,9 +156,13 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_c
 #pragma unroll
       for (int r = 0; r < TR_RPT; ++r) {
         const float x = rs[(hv * TR_RPT + r) * TR_M];
-        hi[r] = tf32_rn(x);
-        lo[r] = tf32_rn(x - hi[r]);
+        split_tf32(x, hi[r], lo[r]);
       }
+      // the split values must exist before the raw slot goes back to the loader: an arrive
+      // issued while the shared loads are still in flight lets the next TMA box land
+      // under them (the compiler may otherwise sink the arithmetic below the arrive)
+#pragma unroll
+      for (int r = 0; r < TR_RPT; ++r) asm volatile("" ::"f"(hi[r]), "f"(lo[r]) : "memory");
       mbar_arrive(&raw_empty[slot]);
       if (!mbar_wait(&op_empty[o], (uo + 1) & 1)) {
         abort_s = 1;
@@ -188,7 +192,7 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_c
     for (long long k = 0; k < my_tiles; ++k) {
       if (abort_s) break;
       const int ab = (int)(k & 1);
-      if (!mbar_wait(&acc_full[ab], (uint32_t)((k >> 1) & 1))) {
+      if (!mbar_wait(&acc_full[ab], (uint32_t)((k >> 1) & 1), 128)) {
         abort_s = 1;
         atomicExch(&g_tc_error, 1);
         break;
@@ -270,7 +274,7 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_c
     for (long long s = 0; s < nstages; ++s) {
       const int slot = (int)(s % TR_RAW);
       if (abort_s) break;
-      if (!mbar_wait(&raw_empty[slot], (uint32_t)(((s / TR_RAW) + 1) & 1))) {
+      if (!mbar_wait(&raw_empty[slot], (uint32_t)(((s / TR_RAW) + 1) & 1), 64)) {
         abort_s = 1;
         atomicExch(&g_tc_error, 1);
         break;
