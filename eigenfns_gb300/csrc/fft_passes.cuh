@@ -36,14 +36,6 @@ constexpr int kThreads = 256;
 #ifndef EF_NRZ_ITEMS
 #define EF_NRZ_ITEMS 256      // z passes: work items per tile
 #endif
-// z passes: CTAs per SM the register allocation must allow. Unbounded, pass A took
-// 102 registers at 128^3 (two CTAs per SM); bounded to three CTAs it takes 80 without
-// spilling and Θ at 128^3 runs 3.56 instead of 3.90 ms for 32 vectors (the
-// preconditioner 3.51 instead of 3.67). The KPM epilogues of pass E keep their
-// registers (they would spill).
-#ifndef EF_ZPASS_MINB
-#define EF_ZPASS_MINB 3
-#endif
 
 template <int R1_, int R2_>
 struct Geo {
@@ -176,7 +168,7 @@ __device__ __forceinline__ void step2_load(const float2* exch, int q, int k1, fl
 // transforms all 3 Cartesian components in registers.
 // grid (G*G/NRA, mb); X points at the sub-batch's first vector.
 template <class GEO, int BUILD>
-__global__ void __launch_bounds__(kThreads, EF_ZPASS_MINB) pass_a_kernel(PassArgs a) {
+__global__ void __launch_bounds__(kThreads) pass_a_kernel(PassArgs a) {
   constexpr int G = GEO::G, NR = GEO::NRA, NP = 3 * NR, R1 = GEO::R1, R2 = GEO::R2;
   extern __shared__ float2 smem[];
   float2* exch = smem;
@@ -345,7 +337,7 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
 // per voxel and the projection happens in registers.
 // grid (G*G/NRE, mb); per-vector pointers (out, X, T0, Y, Z) at the sub-batch start.
 template <class GEO, int EPI>
-__global__ void __launch_bounds__(kThreads, (EPI >= EPI_KPM ? 1 : EF_ZPASS_MINB)) pass_e_kernel(PassArgs a) {
+__global__ void __launch_bounds__(kThreads) pass_e_kernel(PassArgs a) {
   constexpr int G = GEO::G, NR = GEO::NRE, NP = 3 * NR, R1 = GEO::R1, R2 = GEO::R2;
   extern __shared__ float2 smem[];
   float2* exch = smem;
