@@ -54,3 +54,20 @@ def test_status_strings_and_argument_checks_without_gpu(lib):
     assert lib.ef_gram(None, None, 4, 4, 16, None, None, 0, None) == 1
     assert lib.ef_rotate(None, None, None, 0, 4, 16, 0, None) == 1
     assert lib.ef_gram_workspace_bytes(0, 4, 16) == 0
+
+
+def test_tensor_core_gram_host_checks_without_gpu(lib, monkeypatch):
+    """ef_gram_tc rejects misaligned rows, odd K and a short work buffer before any device
+    work; with the packed layout on, A^H B with a 32-row B is planned as (B^H A)^H, so both
+    orders need the same work buffer."""
+    fake_a, fake_b, fake_g, fake_err = 0x10000, 0x20000, 0x30000, 0x40000
+    assert lib.ef_gram_tc(fake_a, fake_b + 8, 4, 4, 16, fake_g, fake_err, None, 0, None) == 1
+    assert lib.ef_gram_tc(fake_a, fake_b, 4, 4, 15, fake_g, fake_err, None, 0, None) == 1
+    assert lib.ef_gram_tc(fake_a, fake_b, 4, 4, 16, fake_g, None, None, 0, None) == 1
+    assert lib.ef_gram_tc(fake_a, fake_b, 32, 32, 4096, fake_g, fake_err, fake_g, 16, None) == 4
+    K = 2 * 64 ** 3
+    monkeypatch.delenv("EF_GRAM_TC_PACK", raising=False)
+    for ma in (40, 96, 200):
+        assert lib.ef_gram_tc_workspace_bytes(ma, 32, K) == lib.ef_gram_tc_workspace_bytes(32, ma, K)
+    monkeypatch.setenv("EF_GRAM_TC_PACK", "0")
+    assert lib.ef_gram_tc_workspace_bytes(96, 32, K) > 0
