@@ -15,7 +15,8 @@ A drop-in for the production path of eigenfns/interior.py of the reference:
   only because a 192^3 basis did not fit a 12 GB card; on GB300 the basis stays
   on the device and the hosted names alias the device versions.
 The bake-off methods (folded spectrum, shift-invert MINRES, expansion polish,
-interior.py:243-307, 468-754) are not part of this build.
+interior.py:243-307, 468-754) live in eigenfns_gb300.bakeoff and are reachable
+under their reference names from this module as well.
 """
 from __future__ import annotations
 
@@ -166,3 +167,15 @@ def bandpass_subspace(op, lam_lo: float, lam_hi: float, lam_max: float, m: int =
 # the hosted variants of the reference exist for 12 GB cards; on GB300 they are the device path
 rr_extract_hosted = rr_extract
 bandpass_subspace_hosted = bandpass_subspace
+
+
+_BAKEOFF = ("FoldedOperator", "folded_subspace", "minres_batched", "shift_invert_subspace",
+            "polish_subspace")
+
+
+def __getattr__(name):
+    """The bake-off methods under their reference names (interior.py:243-754)."""
+    if name in _BAKEOFF:
+        from . import bakeoff
+        return getattr(bakeoff, name)
+    raise AttributeError(f"module {__name__!r} has no attribute {name!r}")

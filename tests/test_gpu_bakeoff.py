@@ -1,0 +1,142 @@
+"""GPU tests of the interior bake-off methods (eigenfns/interior.py:243-754), after the
+reference's own interior tests (tests/test_interior.py:23-77): the folded-operator
+identity, MINRES on the SPD and on an indefinite shift, and the two subspace
+methods against a dense complex128 spectrum on an 8^3 grid."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+G = 16
+
+
+@pytest.fixture(scope="module")
+def op():
+    """A few random eps = 8.41 voxels in eps = 1 on 16^3, box 2 (test_interior.py:23-33)."""
+    from eigenfns_gb300 import _lib
+    from eigenfns_gb300.operator import MaxwellOperator
+    _lib.load()
+    rng = np.random.default_rng(0)
+    eps = np.ones((G, G, G), np.float32)
+    idx = rng.integers(0, G, (60, 3))
+    eps[idx[:, 0], idx[:, 1], idx[:, 2]] = 8.41
+    return MaxwellOperator(eps, 2.0)
+
+
+def _unit_block(op, m, seed):
+    from eigenfns_gb300 import blas
+    from eigenfns_gb300.chebyshev import random_block
+    Z = random_block(op, m, seed, 0x7E57)
+    return blas.scale_rows(Z, 1.0 / blas.row_norms(Z))
+
+
+def _norms(Z):
+    return torch.linalg.vector_norm(Z.reshape(Z.shape[0], -1), dim=1).cpu().numpy()
+
+
+def test_folded_operator_identity(op):
+    """(Θ - σ)^2 x from FoldedOperator equals the composition (test_interior.py:46-55)."""
+    from eigenfns_gb300.interior import FoldedOperator
+    sigma = 1.3
+    fop = FoldedOperator(op, sigma)
+    X = _unit_block(op, 3, 1)
+    Y1 = fop.theta(X)
+    Z = op.theta(X) - sigma * X
+    Y2 = op.theta(Z) - sigma * Z
+    err = float(torch.linalg.vector_norm(Y1 - Y2) / torch.linalg.vector_norm(Y2))
+    assert err < 5e-6
+    assert fop.n_theta == 6
+    out = torch.empty_like(X)
+    assert torch.equal(fop.theta(X, out=out), Y1)
+    P = fop.precondition(X)
+    ref = X * fop._fold_diag
+    assert torch.equal(P, ref)
+
+
+def test_minres_solves_spd(op):
+    """MINRES on Θ (σ = 0, SPD on the transverse space) reaches its tolerance
+    quickly (test_interior.py:58-65)."""
+    from eigenfns_gb300.interior import minres_batched
+    B = _unit_block(op, 2, 2)
+    Y, it, nt = minres_batched(op, B, 0.0, tol=1e-5, maxit=200)
+    R = op.theta(Y) - B
+    assert _norms(R).max() < 1e-3
+    assert it < 100 and nt > 0
+
+
+def test_minres_indefinite_reduces_residual(op):
+    """An indefinite shift: more iterations leave a smaller residual (test_interior.py:68-77)."""
+    from eigenfns_gb300.interior import minres_batched
+    B = _unit_block(op, 2, 3)
+    sigma = 5.0
+    rels = []
+    for maxit in (10, 80):
+        Y, _, _ = minres_batched(op, B, sigma, tol=1e-10, maxit=maxit)
+        R = op.theta(Y) - sigma * Y - B
+        rels.append(float(torch.linalg.vector_norm(R) / torch.linalg.vector_norm(B)))
+    assert rels[1] < rels[0]
+
+
+def _dense8():
+    from eigenfns_gb300.operator import MaxwellOperator
+    from oracle.dense import dense_spectrum
+    from oracle.operator import MaxwellOperator as Ref
+    rng = np.random.default_rng(3)
+    eps = np.asarray(1.0 + 7.57 * (rng.random((8, 8, 8)) > 0.7), np.float32)
+    w = dense_spectrum(Ref(eps, 1.0, dtype=np.complex128))
+    return MaxwellOperator(eps, 1.0), w
+
+
+def test_shift_invert_converges_to_dense_eigenvalues():
+    """Converged Ritz pairs of the shift-invert iteration sit on the dense spectrum."""
+    from eigenfns_gb300.interior import shift_invert_subspace
+    op8, w = _dense8()
+    sigma = 0.5 * (w[5] + w[6])
+    Xr, st = shift_invert_subspace(op8, sigma, m=8, max_outer=12, inner_tol=1e-5,
+                                   inner_maxit=300, res_tol=1e-4, target_count=2, chunk=8,
+                                   verbose=False)
+    lam, res = st["lam"], st["res"]
+    # a Ritz pair with relative residual r lies within r |λ| of the spectrum
+    conv = np.isfinite(lam) & (res < 1e-3)
+    assert conv.sum() >= 2
+    for x, r in zip(lam[conv], res[conv]):
+        assert np.abs(w - x).min() <= 1.01 * r * abs(x) + 1e-6 * abs(x)
+    near = np.sort(np.abs(lam[conv] - sigma))[:2]
+    assert near.max() < 0.5 * (w[7] - w[4])
+    assert Xr.shape == (8, 2, 8, 8, 8) and st["theta_applications"] > 0
+
+
+def test_folded_subspace_runs_and_reports():
+    """LOBPCG on the folded operator: shapes, counters and folded values (its fp32
+    residual floor is what lost it the bake-off, so no convergence bar here)."""
+    from eigenfns_gb300.interior import folded_subspace
+    op8, w = _dense8()
+    sigma = 0.5 * (w[5] + w[6])
+    vecs, st = folded_subspace(op8, sigma, 2, m=6, guard=2, tol=1e-3, maxit=20, verbose=False)
+    assert vecs.shape[0] == 2 and st["method"] == "folded"
+    assert np.isfinite(st["mu"]).all() and (st["mu"] >= -1e-3).all()
+    assert st["theta_applications"] > 0
+
+
+def test_polish_lowers_window_residuals(op):
+    """Preconditioned-residual expansion takes perturbed window eigenvectors back
+    toward convergence (interior.py:468-613)."""
+    from eigenfns_gb300.chebyshev import lanczos_lambda_max
+    from eigenfns_gb300.interior import polish_subspace
+    from eigenfns_gb300.solver import lobpcg_blocks
+    vals, vecs, _ = lobpcg_blocks(op, 8, m=12, guard=4, tol=1e-6, maxit=300, verbose=False)
+    lam_max = 1.05 * lanczos_lambda_max(op)
+    noise = _unit_block(op, 8, 4)
+    X = (vecs + 1e-3 * noise).contiguous()
+    lo, hi = float(vals[1]) - 1e-3, float(vals[6]) + 1e-3
+    Xp, lam, rn, st = polish_subspace(op, X, lo, hi, lam_max, max_sweeps=3, res_tol=1e-5,
+                                      strip_degree=60, strip_every=0, verbose=False)
+    first = st["sweeps"][0]["med_res"]
+    inwin = np.isfinite(lam) & (lam >= lo) & (lam <= hi)
+    assert inwin.sum() >= 4
+    assert float(np.median(rn[inwin])) < first
+    assert Xp.shape == X.shape and st["theta_applications"] > 0
