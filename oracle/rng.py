@@ -7,7 +7,7 @@ The reference draws its start blocks and probes with JAX's threefry
 scripts/exp/exp_kpm_dos.py:139-140). JAX is not available here, so both the
 oracle and the CUDA library use one counter-based generator instead: element i
 of stream s under seed k takes the 64-bit word mix(key(k, s) + (i+1)·φ) with
-the splitmix64 finaliser. Parity against the reference is therefore judged on
+the splitmix64 finaliser. Parity against the reference is therefore assessed on
 converged results, never on the random stream itself. The CUDA kernel
 (`eigenfns_gb300/csrc/blas.cu`, `rng_key`/`rng_word`) computes the same words;
 its float32 Box-Muller transform agrees with this one to a few ulp.
