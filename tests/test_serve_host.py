@@ -1,0 +1,111 @@
+"""Host logic of the request server on the CPU: admission by device-memory footprint,
+the concurrency cap, arrival order, error surfacing and the same results served as
+plain. The solve itself is replaced by a deterministic stand-in (the real one runs in
+tests/test_gpu_serve.py)."""
+from __future__ import annotations
+
+import contextlib
+import threading
+import time
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+
+class _Stream:
+    def __init__(self, device=None):
+        pass
+
+    def synchronize(self):
+        pass
+
+
+@pytest.fixture()
+def fake_server(monkeypatch):
+    from eigenfns_gb300 import blas, serve
+    monkeypatch.setattr(torch.cuda, "Stream", _Stream)
+    monkeypatch.setattr(torch.cuda, "device", lambda d: contextlib.nullcontext())
+    monkeypatch.setattr(torch.cuda, "stream", lambda s: contextlib.nullcontext())
+    monkeypatch.setattr(torch.cuda, "synchronize", lambda d=None: None)
+    monkeypatch.setattr(blas, "release_workspaces", lambda stream=None: None)
+    state = {"running": 0, "peak": 0, "lock": threading.Lock()}
+
+    class _Stats:
+        def __init__(self, req):
+            self.rounds = [{"max_res_locked": 1e-5}]
+            self.theta_applications = 10 * req.nev
+            self.iterations = req.nev
+
+    def fake_solve(req, device):
+        with state["lock"]:
+            state["running"] += 1
+            state["peak"] = max(state["peak"], state["running"])
+        if req.seed < 0:
+            with state["lock"]:
+                state["running"] -= 1
+            raise RuntimeError("planted failure")
+        time.sleep(0.02)
+        vals = np.sort(np.random.default_rng(req.seed).random(req.nev)) + req.grid
+        with state["lock"]:
+            state["running"] -= 1
+        return vals, _Stats(req)
+
+    monkeypatch.setattr(serve, "_solve_one", fake_solve)
+    return serve, state
+
+
+def _requests(serve, n=12):
+    return [serve.SolveRequest(rid=i, nodes=64, grid=32 if i % 3 else 48, seed=100 + i,
+                               nev=8 + (i % 5), arrival=0.005 * i) for i in range(n)]
+
+
+def test_admission_respects_budget_and_concurrency(fake_server):
+    serve, state = fake_server
+    reqs = [serve.SolveRequest(rid=i, nodes=64, grid=32, seed=100 + i, nev=12, arrival=0.002 * i)
+            for i in range(10)]
+    fp = serve.footprint_bytes(reqs[0])
+    srv = serve.EigenServer(budget_bytes=2.5 * fp, max_concurrent=4, device="cpu")
+    res = srv.run(reqs, realtime=True)           # memory admits two at a time
+    assert [r.rid for r in res] == list(range(len(reqs)))
+    assert srv.peak_used <= 2.5 * fp and srv.peak_concurrent == 2 and state["peak"] <= 2
+    assert all(r.start >= r.arrival - 1e-6 and r.end >= r.start for r in res)
+    state["peak"] = 0
+    mixed = _requests(serve)
+    srv = serve.EigenServer(budget_bytes=1e15, max_concurrent=3, device="cpu")
+    res = srv.run(mixed, realtime=False)         # the slot cap binds
+    assert len(res) == len(mixed) and srv.peak_concurrent <= 3 and state["peak"] <= 3
+
+
+def test_served_results_equal_plain(fake_server):
+    serve, _ = fake_server
+    reqs = _requests(serve, 8)
+    served = serve.EigenServer(budget_bytes=1e15, max_concurrent=8, device="cpu").run(reqs,
+                                                                                      realtime=False)
+    plain = serve.run_plain(reqs, device="cpu")
+    for a, b in zip(served, plain):
+        assert a.rid == b.rid and np.array_equal(a.vals, b.vals)
+    s = serve.summarize(served, 1.0)
+    assert s["modes"] == sum(r.nev for r in reqs) and s["p99_latency_s"] >= s["p50_latency_s"]
+
+
+def test_oversized_request_and_failures_are_reported(fake_server):
+    serve, _ = fake_server
+    reqs = _requests(serve, 4)
+    with pytest.raises(ValueError):
+        serve.EigenServer(budget_bytes=1.0, device="cpu").run(reqs)
+    reqs[2].seed = -1                        # planted failure inside one solve
+    with pytest.raises(RuntimeError, match="1 request"):
+        serve.EigenServer(budget_bytes=1e15, device="cpu").run(reqs, realtime=False)
+
+
+def test_request_stream_is_seeded():
+    from eigenfns_gb300 import serve
+    a = serve.poisson_requests(20, seed=5, rate_hz=40.0)
+    b = serve.poisson_requests(20, seed=5, rate_hz=40.0)
+    assert [(r.grid, r.nev, r.k_frac, r.arrival) for r in a] == \
+           [(r.grid, r.nev, r.k_frac, r.arrival) for r in b]
+    assert all(a[i].arrival < a[i + 1].arrival for i in range(19))
+    assert all(-0.5 <= x < 0.5 for r in a for x in r.k_frac)
+    assert all(8 <= r.nev <= 48 and r.grid in (32, 48, 64) for r in a)
