@@ -195,10 +195,10 @@ def run_reference(args, w):
     return 0
 
 
-# The GPU solve of this workload takes 394 LOBPCG iterations in 9 blocks (measured on
+# The GPU solve of this workload takes 381 LOBPCG iterations in 9 blocks (measured on
 # a GB300; the oracle's per-iteration cost is extrapolated with these counts when the
 # reference arm runs alone)
-GPU_SOLVE_PROFILE = {"iterations": 394, "blocks": 9}
+GPU_SOLVE_PROFILE = {"iterations": 381, "blocks": 9}
 
 
 def _solve_profile():
