@@ -124,6 +124,7 @@ def folded_subspace(op, sigma: float, nev: int, m: int = 64, guard: int = 14, to
                                    theta_chunk=theta_chunk, seed=seed, verbose=verbose,
                                    log_every=log_every, locked_storage="host")
     wall = time.perf_counter() - t0
+    blas.raise_on_tc_error("folded_subspace")
     return vecs, {"method": "folded", "sigma": sigma, "mu": np.asarray(vals),
                   "theta_applications": fop.n_theta, "wall_seconds": wall,
                   "outer_stats": st.rounds}
@@ -256,6 +257,7 @@ def shift_invert_subspace(op, sigma: float, m: int = 64, max_outer: int = 12,
             break
         best = max(best, int(conv.sum()))
         X = Xr
+    blas.raise_on_tc_error("shift_invert_subspace")
     return Xr, {"method": "shift_invert", "sigma": sigma, "m": m, "theta_applications": n_theta,
                 "wall_seconds": time.perf_counter() - t0, "outer_stats": hist,
                 "lam": lam, "res": rn}
@@ -338,5 +340,6 @@ def polish_subspace(op, X, lam_lo: float, lam_hi: float, lam_max: float, max_swe
             del outs
         lam, X, rn = rr_extract(op, X, theta_chunk)
         n_theta += 2 * m
+    blas.raise_on_tc_error("polish_subspace")
     return X, lam, rn, {"method": "polish", "theta_applications": n_theta,
                         "wall_seconds": time.perf_counter() - t0, "sweeps": hist}

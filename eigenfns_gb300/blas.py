@@ -129,6 +129,14 @@ def tc_error() -> int:
     return int(flag.value)
 
 
+def raise_on_tc_error(what: str) -> None:
+    """Raise RuntimeError if a tensor-core kernel's bounded pipeline wait ran out since the
+    last check (the results computed since then are not valid). Synchronises."""
+    if tc_error():
+        raise RuntimeError(f"{what}: a tensor-core kernel timed out waiting on its pipeline; "
+                           "results invalid")
+
+
 def combine(C, *blocks: torch.Tensor) -> torch.Tensor:
     Cd = _coef(C, blocks[0].device)
     out = None

@@ -16,7 +16,7 @@ from dataclasses import dataclass, field
 import numpy as np
 import torch
 
-from . import blas
+from . import blas, chebcoef
 from ._lib import EF_RAND_NORMAL, EF_RAND_RADEMACHER, EF_RAND_RADEMACHER_C, call
 from .blas import combine, deflate, gram
 from .solver import deflate_chunk_rows, ortho_block
@@ -165,22 +165,14 @@ def chebsi_bottom_up(op, nev: int, guard: int = 48, degree: int = 200, tol: floa
             print(f"  outer {outer:2d}: locked {n_locked:4d}/{nev}  lam_c {lam_c:8.4f}", flush=True)
         if n_locked >= nev:
             break
+    blas.raise_on_tc_error("chebsi_bottom_up")
     stats.wall_seconds = time.perf_counter() - t0
     return lam[:nev], X[:nev], stats
 
 
 def step_jackson_coeffs(lam_b: float, lam_max: float, degree: int) -> np.ndarray:
     """Jackson-damped Chebyshev coefficients of 1_{λ<λ_b} (chebyshev.py:232-242)."""
-    xb = (2 * lam_b - lam_max) / lam_max
-    ks = np.arange(degree + 1)
-    tb = np.arccos(np.clip(xb, -1, 1))
-    mu = np.empty(degree + 1)
-    mu[0] = 1 - tb / np.pi
-    mu[1:] = -2 * np.sin(ks[1:] * tb) / (ks[1:] * np.pi)
-    g = ((degree - ks + 1) * np.cos(np.pi * ks / (degree + 1))
-         + np.sin(np.pi * ks / (degree + 1)) / np.tan(np.pi / (degree + 1)))
-    g /= (degree + 1)
-    return mu * g
+    return chebcoef.damped_step(lam_b, lam_max, degree)
 
 
 def kpm_count_below(op, lam_b: float, lam_max: float, degree: int = 500, n_probe: int = 30,
@@ -215,4 +207,5 @@ def kpm_count_below(op, lam_b: float, lam_max: float, degree: int = 500, n_probe
         prev, cur = cur, prev
     op.n_theta += degree * n_probe
     per_probe = est.cpu().numpy()
+    blas.raise_on_tc_error("kpm_count_below")
     return float(per_probe.mean()), float(per_probe.std(ddof=1) / np.sqrt(n_probe))

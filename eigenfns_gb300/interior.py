@@ -25,7 +25,7 @@ import time
 import numpy as np
 import torch
 
-from . import blas
+from . import blas, chebcoef
 from ._lib import call
 from .blas import combine, gram
 from .chebyshev import random_block
@@ -68,30 +68,15 @@ def rr_extract(op, X, theta_chunk: int = 8):
     bad = np.sqrt(np.maximum(st[2], 0)) < 0.5
     lam = np.where(bad, np.inf, lam)
     rn = np.where(bad, np.inf, rn)
+    blas.raise_on_tc_error("rr_extract")
     return lam, Xr, rn
 
 
-def _jackson(p: int) -> np.ndarray:
-    k = np.arange(p + 1)
-    g = ((p - k + 1) * np.cos(np.pi * k / (p + 1))
-         + np.sin(np.pi * k / (p + 1)) / np.tan(np.pi / (p + 1)))
-    return g / (p + 1)
-
-
-def _step_coeffs(xb: float, p: int) -> np.ndarray:
-    k = np.arange(1, p + 1)
-    tb = np.arccos(np.clip(xb, -1.0, 1.0))
-    c = np.empty(p + 1)
-    c[0] = 1 - tb / np.pi
-    c[1:] = -2 * np.sin(k * tb) / (k * np.pi)
-    return c
-
-
-def bandpass_coeffs(lam_lo: float, lam_hi: float, lam_max: float, degree: int) -> np.ndarray:
-    """Jackson-damped Chebyshev coefficients of 1_{lam_lo < λ < lam_hi}."""
-    x_lo = 2 * lam_lo / lam_max - 1
-    x_hi = 2 * lam_hi / lam_max - 1
-    return _jackson(degree) * (_step_coeffs(x_hi, degree) - _step_coeffs(x_lo, degree))
+# The reference's names for the filter coefficients (interior.py:312-333); one
+# implementation in chebcoef serves the filters, the count and the KPM analysis.
+_jackson = chebcoef.jackson_damping
+_step_coeffs = chebcoef.step_below
+bandpass_coeffs = chebcoef.bandpass
 
 
 def _apply_cheb_poly(op, X, coef, lam_max: float):
@@ -159,6 +144,7 @@ def bandpass_subspace(op, lam_lo: float, lam_hi: float, lam_max: float, m: int =
             break
         best = max(best, int(conv.sum()))
         X = Xr
+    blas.raise_on_tc_error("bandpass_subspace")
     return Xr, {"method": "bandpass", "degree": degree, "m": m, "lam_window": (lam_lo, lam_hi),
                 "theta_applications": n_theta, "wall_seconds": time.perf_counter() - t0,
                 "outer_stats": hist, "lam": lam, "res": rn}

@@ -20,6 +20,7 @@ import time
 import numpy as np
 import torch
 
+from . import blas
 from .chebyshev import lanczos_lambda_max
 from .interior import _apply_cheb_poly, bandpass_coeffs, bandpass_subspace, rr_extract
 
@@ -95,6 +96,7 @@ def two_stage(op, lam_lo: float, lam_hi: float, m: int, lam_max: float = 0.0,
     idx = np.where(conv)[0][np.argsort(lam[conv], kind="stable")]
     uidx = np.where(unconv)[0][np.argsort(lam[unconv], kind="stable")]
     dev_idx = torch.from_numpy(idx).to(X.device)
+    blas.raise_on_tc_error("two_stage")
     return {"vals": lam[idx], "res": rn[idx], "vecs": X.index_select(0, dev_idx),
             "unconverged_vals": lam[uidx], "unconverged_res": rn[uidx],
             "lam": lam, "rn": rn, "lam_max": lam_max, "n_converged": int(conv.sum()),

@@ -3,7 +3,7 @@
  * A thin, stream-ordered C interface over hand-written sm_103a CUDA kernels. It
  * replaces the device work of the reference (fhernandez93/eigenfns, JAX/XLA);
  * every entry names the reference code it stands in for. The Python package
- * `eigenfns_gb300` binds it with ctypes; INTEGRATION.md shows the binding.
+ * `eigenfns_gb300` binds it with ctypes (eigenfns_gb300/_lib.py).
  *
  * Conventions
  *   - Complex64 arrays are interleaved (re, im) float pairs; complex128 arrays
@@ -142,14 +142,17 @@ int ef_gram(const float* A, const float* B, int ma, int mb, long long K, double*
  * serialised by the caller. Allocates nothing. */
 int ef_gram_noalloc(const float* A, const float* B, int ma, int mb, long long K, double* G,
                     void* stream);
-/* the same Gram on the tcgen05 tensor cores: 3xTF32 split products (fp32-class accuracy),
- * fp32 accumulation in TMEM per K-chunk, fp64 reduction across chunks. mb <= 256, K even,
- * 16-byte aligned rows. err_dev (device int) is set to 1 if a bounded wait timed out. */
 /* reads and clears the sticky device flag the tensor-core rotation sets when one of its
  * bounded waits ran out (never expected; results of that call are not valid).
  * Synchronises the device. */
 int ef_tc_error(int* flag);
+/* work bytes of ef_gram_tc for these sizes */
 size_t ef_gram_tc_workspace_bytes(int ma, int mb, long long K);
+/* the Gram of ef_gram (solver.py:35-43) on the tcgen05 tensor cores: 3xTF32 split
+ * products (fp32-class accuracy), fp32 accumulation in TMEM per K-chunk, fp64 reduction
+ * across chunks. mb <= 256, K even, 16-byte aligned rows. err_dev (a device int, not
+ * NULL) is set to 1 if a bounded wait timed out (never expected; the result of that call
+ * is then not valid). */
 int ef_gram_tc(const float* A, const float* B, int ma, int mb, long long K, double* G, int* err_dev,
                void* work, size_t work_bytes, void* stream);
 /* out_i (+/-)= sum_j C[j][i] S_j, C complex64 (m_in, m_out) row-major:

@@ -1,12 +1,12 @@
 """Small, self-contained kernel workloads for profiling (ncu) and quick timing.
 
-    python -m eigenfns_gb300.profile_kernels theta --grid 128 --m 2
-    python -m eigenfns_gb300.profile_kernels gram --ma 32 --mb 32 --grid 128
-    python -m eigenfns_gb300.profile_kernels gram_tc --ma 32 --mb 32 --grid 128
-    python -m eigenfns_gb300.profile_kernels rotate --ma 96 --mb 64 --grid 128
-    python -m eigenfns_gb300.profile_kernels cheb --grid 192 --m 8 --steps 8
-    python -m eigenfns_gb300.profile_kernels kpm --grid 256 --m 4 --steps 8
-    python -m eigenfns_gb300.profile_kernels rowstats --ma 32 --mb 32 --grid 128
+    python profile_kernels.py theta --grid 128 --m 2
+    python profile_kernels.py gram --ma 32 --mb 32 --grid 128
+    python profile_kernels.py gram_tc --ma 32 --mb 32 --grid 128
+    python profile_kernels.py rotate --ma 96 --mb 64 --grid 128
+    python profile_kernels.py cheb --grid 192 --m 8 --steps 8
+    python profile_kernels.py kpm --grid 256 --m 4 --steps 8
+    python profile_kernels.py rowstats --ma 32 --mb 32 --grid 128
 
 Each runs 3 warm-up calls and then one timed call (CUDA events on the current
 stream), printing the time; under ncu, skip the warm-up launches with -s.
@@ -21,7 +21,7 @@ import torch
 
 
 def _op(G: int):
-    from .operator import MaxwellOperator
+    from eigenfns_gb300.operator import MaxwellOperator
     rng = np.random.default_rng(0)
     eps = np.asarray(1.0 + 7.41 * (rng.random((G, G, G)) > 0.78), np.float32)
     return MaxwellOperator(eps, 5.0)
@@ -60,15 +60,15 @@ def main(argv=None) -> None:
         elif a.kernel == "precond":
             ms = _timed(lambda: op.precondition(X, out=Y))
         elif a.kernel == "cheb":
-            from .interior import _apply_cheb_poly
+            from eigenfns_gb300.interior import _apply_cheb_poly
             coef = np.linspace(1.0, 0.1, a.steps + 1)
             ms = _timed(lambda: _apply_cheb_poly(op, X, coef, 4.0e4))
         else:
-            from .kpm import kpm_moments
+            from eigenfns_gb300.kpm import kpm_moments
             ms = _timed(lambda: kpm_moments(op, 4.0e4, 2 * a.steps, a.m, Z=X))
         print(f"{a.kernel} grid {G} m {a.m}: {ms:.3f} ms")
     else:
-        from . import blas
+        from eigenfns_gb300 import blas
         K = 2 * G ** 3
         A = torch.randn((a.ma, K), dtype=torch.complex64, device="cuda", generator=g)
         B = torch.randn((a.mb, K), dtype=torch.complex64, device="cuda", generator=g)

@@ -1,8 +1,10 @@
 """Generate the golden fixtures by executing the reference's own code.
 
-Run in the development container (the reference checkout must be present):
+Run in the development container (the reference checkout must be present;
+its path is the first argument or $EIGENFNS_REFERENCE):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference checkout>          # reference_golden.npz
+    python tests/golden/make_golden.py <reference checkout> --kpm    # reference_kpm_golden.npz
 
 JAX is not installed there, so `jax_standin` maps jax.numpy onto numpy and
 records every random draw; the reference modules (eigenfns/operator.py,
@@ -213,6 +215,58 @@ def main(ref_root: str):
     print(f"wrote {dest} ({dest.stat().st_size / 1024:.0f} KiB, {len(out)} arrays)")
 
 
+def main_kpm(ref_root: str):
+    """KPM analysis (scripts/exp/exp_kpm_analyze.py:39-64) and the deflated-probe
+    completeness count (eigenfns/chebyshev.py:213-267 with `locked`)."""
+    ref = Path(ref_root)
+    sys.path.insert(0, str(ref))
+    import jax.numpy as jnp
+    from eigenfns.operator import MaxwellOperator
+    from eigenfns import chebyshev as rcheb
+    from eigenfns import solver as rsolver
+    ka = _load(ref / "scripts/exp/exp_kpm_analyze.py", "exp_kpm_analyze")
+    out = {}
+    rng = np.random.default_rng(4321)
+
+    # analysis of a moment table: decaying per-probe moments, as a DOS produces
+    for tag, (probes, p, lmax, n_pts) in {"ka0": (6, 120, 40.0, 500),
+                                          "ka1": (4, 1500, 2208.9, 400)}.items():
+        k = np.arange(p + 1)
+        mom = rng.standard_normal((probes, p + 1)) / (1.0 + 0.05 * k) + np.cos(0.3 * k)
+        mom[:, 0] = 2 * 8 ** 3 - 2
+        lams = np.linspace(0.05 * lmax, 0.95 * lmax, 9)
+        out[f"{tag}_mom"] = mom
+        out[f"{tag}_args"] = np.asarray([lmax, n_pts], np.float64)
+        out[f"{tag}_lams"] = lams
+        mean, se, est = ka.counting(mom, lmax, lams)
+        out[f"{tag}_count_mean"], out[f"{tag}_count_se"], out[f"{tag}_count_est"] = mean, se, est
+        lam, rho = ka.dos_curve(mom, lmax, n_pts=n_pts)
+        out[f"{tag}_dos_lam"], out[f"{tag}_dos_rho"] = lam, rho
+        out[f"{tag}_smear"] = ka.smearing_width(lams, lmax, p)
+
+    # deflated-probe count on the 8^3 operator of the main fixture set
+    eps = disordered_eps(8, 0)
+    op64 = MaxwellOperator(eps, 1.0, dtype=jnp.complex64)
+    vals, vecs, _ = rsolver.lobpcg_blocks(op64, 12, m=8, guard=3, tol=1e-5, maxit=300,
+                                         verbose=False)
+    lam_b = float(0.5 * (vals[5] + vals[6]))          # six eigenvalues below lam_b
+    locked = np.asarray(vecs)[:6]
+    lam_max = 1.05 * rcheb.lanczos_lambda_max(op64, iters=24, seed=3, n_seeds=1)
+    for tag, lk in (("kd_plain", None), ("kd_defl", locked)):
+        jax_standin.DRAWS.clear()
+        mean, se = rcheb.kpm_count_below(op64, lam_b, lam_max, degree=80, n_probe=6, seed=5,
+                                         locked=None if lk is None else jnp.asarray(lk))
+        out[f"{tag}_Z"] = np.where(jax_standin.DRAWS[0][1], 1.0, -1.0).astype(np.complex64)
+        out[f"{tag}_out"] = np.asarray([mean, se, lam_b, lam_max, 80, 6], np.float64)
+    out["kd_eps"] = eps
+    out["kd_locked"] = locked
+    out["kd_vals"] = np.asarray(vals)
+
+    dest = HERE / "reference_kpm_golden.npz"
+    np.savez_compressed(dest, **out)
+    print(f"wrote {dest} ({dest.stat().st_size / 1024:.0f} KiB, {len(out)} arrays)")
+
+
 def _load(path: Path, name: str):
     import importlib.util
     spec = importlib.util.spec_from_file_location(name, path)
@@ -222,4 +276,9 @@ def _load(path: Path, name: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("EIGENFNS_REFERENCE", ""))
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    root = args[0] if args else os.environ.get("EIGENFNS_REFERENCE", "")
+    if "--kpm" in sys.argv:
+        main_kpm(root)
+    else:
+        main(root)

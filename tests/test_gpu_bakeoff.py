@@ -112,14 +112,25 @@ def test_shift_invert_converges_to_dense_eigenvalues():
 
 def test_folded_subspace_runs_and_reports():
     """LOBPCG on the folded operator: shapes, counters and folded values (its fp32
-    residual floor is what lost it the bake-off, so no convergence bar here)."""
+    residual floor is what lost it the bake-off, so no convergence bar here). The
+    folded values must respect the dense folded spectrum: Ritz values of (Θ - σ)^2
+    interlace above its sorted eigenvalues, and each one bounds the square of its
+    vector's shifted Rayleigh quotient from above (a wrong shift or fold breaks both)."""
+    from eigenfns_gb300 import blas
     from eigenfns_gb300.interior import folded_subspace
     op8, w = _dense8()
     sigma = 0.5 * (w[5] + w[6])
     vecs, st = folded_subspace(op8, sigma, 2, m=6, guard=2, tol=1e-3, maxit=20, verbose=False)
     assert vecs.shape[0] == 2 and st["method"] == "folded"
-    assert np.isfinite(st["mu"]).all() and (st["mu"] >= -1e-3).all()
+    mu = np.asarray(st["mu"])
+    assert np.isfinite(mu).all() and (mu >= -1e-3).all()
     assert st["theta_applications"] > 0
+    folded = np.sort((w - sigma) ** 2)
+    scale = folded[-1]
+    assert np.all(np.sort(mu) >= folded[:mu.size] - 1e-5 * scale)
+    hv = op8.theta(vecs)
+    rq = (blas.rowdot(vecs, hv).real / blas.rowdot(vecs, vecs).real).cpu().numpy()
+    assert np.all(mu >= (rq - sigma) ** 2 - 1e-5 * scale)
 
 
 def test_polish_lowers_window_residuals(op):

@@ -104,6 +104,22 @@ def test_kpm_count_matches_reference(golden, gpu):
     assert s2 == pytest.approx(se, abs=1e-3)
 
 
+@pytest.mark.parametrize("tag", ["kd_plain", "kd_defl"])
+def test_kpm_count_deflated_probes_match_reference(tag, gpu):
+    """Completeness-gate mode (chebyshev.py:221-252): probes deflated twice against the
+    locked eigenvectors below λ_b, against the reference's run on the same probes."""
+    from pathlib import Path
+    from eigenfns_gb300.chebyshev import kpm_count_below
+    from eigenfns_gb300.operator import MaxwellOperator
+    kg = np.load(Path(__file__).resolve().parent / "golden" / "reference_kpm_golden.npz")
+    op = MaxwellOperator(kg["kd_eps"], 1.0)
+    mean, se, lb, lmax, deg, npb = kg[f"{tag}_out"]
+    locked = kg["kd_locked"] if tag == "kd_defl" else None
+    m2, s2 = kpm_count_below(op, lb, lmax, degree=int(deg), Z=kg[f"{tag}_Z"], locked=locked)
+    assert m2 == pytest.approx(mean, abs=1e-3)
+    assert s2 == pytest.approx(se, abs=1e-3)
+
+
 def test_kpm_moments_match_reference(golden, gpu):
     from eigenfns_gb300.kpm import kpm_moments
     from eigenfns_gb300.operator import MaxwellOperator
