@@ -1,0 +1,141 @@
+"""The interior-window workload at its full size, end to end on one GPU.
+
+    python bench_interior.py kpm      [--degree 12000 --probes 16 --grid 256]
+    python bench_interior.py chebsi   [--grid 192 --m 104 --build-outers 2 --polish-outers 4]
+
+Structure: the seeded tetravalent rod network with N = 10,000 nodes (eps_rod 8.41,
+sub-voxel averaged), the reference's interior case.
+
+kpm     KPM density of states at 256^3, Γ: λ_max from 24-step Lanczos (x1.05),
+        degree 12000 (6001 operator steps per probe with the doubling identities),
+        16 complex Rademacher probes projected to the transverse subspace, Jackson
+        kernel (scripts/exp/exp_kpm_dos.py:125-163, exp_kpm_analyze.py). Prints the
+        wall time, operator applications and the counting function; writes the
+        per-probe moments to --out.
+chebsi  Two-stage bandpass ChebSI at 192^3 with m = 104: build degree 3000 x 2
+        outers, polish degree 12000 x up to 4 outers, stopping when every in-window
+        pair converged (scripts/run_interior.py:154-216). The reference's window
+        [1.757, 1.930] is in its own units (µm^-2 for its structures), so the window
+        here keeps its relative width (λ_hi/λ_lo = 1.098) and is placed where this
+        structure's KPM counting function (a 192^3 estimate, 8 probes, degree 2000)
+        gives about 69 modes inside, the size of the reference's S_below window.
+
+Each run prints one JSON line with its measurements.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+SEED = 7          # structure seed of the interior workload
+WINDOW_RATIO = 1.930 / 1.757
+
+
+def _operator(grid: int):
+    from eigenfns_gb300.operator import MaxwellOperator
+    from eigenfns_gb300.structure import make_structure
+    eps, L, net = make_structure(10000, grid, seed=SEED)
+    return MaxwellOperator(eps, L), net
+
+
+def run_kpm(a) -> dict:
+    import torch
+    from eigenfns_gb300 import kpm
+    from eigenfns_gb300.chebyshev import lanczos_lambda_max
+    t0 = time.perf_counter()
+    op, net = _operator(a.grid)
+    lam_max = 1.05 * lanczos_lambda_max(op)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    mom = kpm.kpm_moments(op, lam_max, a.degree, a.probes, seed=a.seed, probe_kind="complex")
+    t2 = time.perf_counter()
+    n_theta = a.probes * (a.degree // 2 + 1)
+    lams = np.linspace(0.02, 0.6, 30) * lam_max
+    mean, se, _ = kpm.counting(mom, lam_max, lams)
+    if a.out:
+        np.savez_compressed(a.out, moments=mom, lam_max=lam_max, grid=a.grid, degree=a.degree,
+                            probes=a.probes, seed=a.seed)
+    G = a.grid
+    return {"workload": f"KPM DOS N=10000 {G}^3 degree {a.degree} x {a.probes} complex probes",
+            "lam_max": lam_max, "setup_s": t1 - t0, "moments_s": t2 - t1,
+            "theta_applications": n_theta, "theta_per_s": n_theta / (t2 - t1),
+            "algorithmic_GBs": 48.0 * G ** 3 * n_theta / (t2 - t1) / 1e9,
+            "counting": {"lam": lams.tolist(), "N": mean.tolist(), "se": se.tolist()}}
+
+
+def choose_window(op, lam_max: float, target: int = 69, probes: int = 8, degree: int = 2000):
+    """(λ_lo, λ_hi) with λ_hi = 1.098 λ_lo and about `target` modes inside (KPM count)."""
+    from eigenfns_gb300 import kpm
+    mom = kpm.kpm_moments(op, lam_max, degree, probes, seed=11, probe_kind="complex")
+    lo = np.linspace(0.005, 0.5, 400) * lam_max
+    n_lo, _, _ = kpm.counting(mom, lam_max, lo)
+    n_hi, _, _ = kpm.counting(mom, lam_max, lo * WINDOW_RATIO)
+    inside = n_hi - n_lo
+    j = int(np.argmin(np.abs(inside - target)))
+    return float(lo[j]), float(lo[j] * WINDOW_RATIO), float(inside[j]), float(n_lo[j])
+
+
+def run_chebsi(a) -> dict:
+    import torch
+    from eigenfns_gb300.chebyshev import lanczos_lambda_max
+    from eigenfns_gb300.run_interior import two_stage
+    t0 = time.perf_counter()
+    op, net = _operator(a.grid)
+    lam_max = 1.05 * lanczos_lambda_max(op)
+    lam_lo, lam_hi, est_inside, est_below = choose_window(op, lam_max)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    r = two_stage(op, lam_lo, lam_hi, a.m, lam_max=lam_max, build_degree=a.build_degree,
+                  build_outers=a.build_outers, polish_degree=a.polish_degree,
+                  polish_outers=a.polish_outers, tol=a.tol, chunk=a.chunk, seed=a.seed,
+                  verbose=True)
+    t2 = time.perf_counter()
+    G = a.grid
+    return {"workload": (f"two-stage ChebSI N=10000 {G}^3 m={a.m} build {a.build_degree}x"
+                         f"{a.build_outers} polish {a.polish_degree}x{a.polish_outers}"),
+            "window": [lam_lo, lam_hi], "kpm_estimate_inside": est_inside,
+            "kpm_estimate_below": est_below, "lam_max": lam_max, "setup_s": t1 - t0,
+            "solve_s": t2 - t1, "theta_applications": r["theta_applications"],
+            "theta_per_s": r["theta_applications"] / (t2 - t1),
+            "n_converged": r["n_converged"], "n_inwindow_unconverged": r["n_inwindow_unconverged"],
+            "vals": np.asarray(r["vals"]).tolist(), "res": np.asarray(r["res"]).tolist(),
+            "history": r["history"]}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("what", choices=["kpm", "chebsi"])
+    ap.add_argument("--grid", type=int, default=None)
+    ap.add_argument("--degree", type=int, default=12000)
+    ap.add_argument("--probes", type=int, default=16)
+    ap.add_argument("--m", type=int, default=104)
+    ap.add_argument("--build-degree", type=int, default=3000)
+    ap.add_argument("--build-outers", type=int, default=2)
+    ap.add_argument("--polish-degree", type=int, default=12000)
+    ap.add_argument("--polish-outers", type=int, default=4)
+    ap.add_argument("--tol", type=float, default=1e-4)
+    ap.add_argument("--chunk", type=int, default=26)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--out", default=None)
+    a = ap.parse_args()
+    import torch
+    torch.cuda.set_device(0)
+    if a.what == "kpm":
+        a.grid = a.grid or 256
+        res = run_kpm(a)
+    else:
+        a.grid = a.grid or 192
+        res = run_chebsi(a)
+    print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()

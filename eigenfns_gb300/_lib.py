@@ -34,6 +34,8 @@ SIGNATURES = {
     "ef_supported_grid": (_i, [_i]),
     "ef_op_create": (_i, [_i, _d, _d, _d, _d, _vp, C.POINTER(_vp)]),
     "ef_op_destroy": (_i, [_vp]),
+    "ef_op_configure": (_i, [_vp, _i, _sz]),
+    "ef_op_pipeline": (_i, [_vp]),
     "ef_op_info": (_i, [_vp, C.POINTER(_i), C.POINTER(_d), C.POINTER(_d)]),
     "ef_op_basis": (_i, [_vp, _vp, _vp, _vp]),
     "ef_op_mask": (_i, [_vp, _vp, _vp]),
@@ -54,6 +56,8 @@ SIGNATURES = {
     "ef_gram_noalloc": (_i, [_vp, _vp, _i, _i, _ll, _vp, _vp]),
     "ef_gram_tc_workspace_bytes": (_sz, [_i, _i, _ll]),
     "ef_tc_error": (_i, [_vp]),
+    "ef_tune_gram": (_i, [_i, _i, _i, _i]),
+    "ef_tune_reset": (_i, []),
     "ef_energy_workspace_bytes": (_i, [_vp, _i]),
     "ef_energy_density": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _sz, _vp]),
     "ef_gram_tc": (_i, [_vp, _vp, _i, _i, _ll, _vp, _vp, _vp, _sz, _vp]),

@@ -10,6 +10,9 @@ float64 device tensors. Every kernel is the library's; there is no fallback.
 """
 from __future__ import annotations
 
+import os
+from contextlib import contextmanager
+
 import numpy as np
 import torch
 
@@ -41,6 +44,40 @@ def release_workspaces(stream=None) -> None:
     sid = None if stream is None else stream.cuda_stream
     for key in [k for k in _WS if sid is None or k[2] == sid]:
         del _WS[key]
+
+
+PRECISIONS = ("mixed", "fp32")
+
+
+@contextmanager
+def precision(mode: str):
+    """Select the arithmetic of the Gram matrices and block rotations inside the block.
+
+    "mixed" (the default): tcgen05 tensor cores with 3xTF32 split products (fp32
+    accumulation in TMEM, fp64 across K-chunks for the Gram). "fp32": CUDA-core
+    kernels with plain fp32 products (fp64 split-K reduction for the Gram). The
+    operator, preconditioner and recurrences are fp32 in both. The library reads the
+    choice at every call (EF_GRAM_KERNEL / EF_ROTATE_KERNEL), so it applies to work
+    issued inside the block from this process.
+    """
+    if mode not in PRECISIONS:
+        raise ValueError(f"precision must be one of {PRECISIONS}, got {mode!r}")
+    keys = ("EF_GRAM_KERNEL", "EF_ROTATE_KERNEL")
+    saved = {k: os.environ.get(k) for k in keys}
+    try:
+        if mode == "fp32":
+            os.environ["EF_GRAM_KERNEL"] = "simt"
+            os.environ["EF_ROTATE_KERNEL"] = "simt"
+        else:
+            for k in keys:
+                os.environ.pop(k, None)
+        yield
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
 
 
 def _c64(x: torch.Tensor) -> torch.Tensor:

@@ -697,6 +697,7 @@ int noalloc_scratch(void** out) {
 inline bool gram_use_tc(int ma, int mb) { return (long long)ma * mb >= 16 * 32; }
 
 namespace ef {
+bool gram_tune_get(int ma, int mb, int* kernel, int* units);
 int* tc_error_dev();
 int tc_rotate_max_rows(int m_out, int mode);
 int tc_rotate_launch(const float* C, int ldc, const float* S, float* out, int m_in, int m_out,
@@ -719,8 +720,10 @@ int ef_gram(const float* A, const float* B, int ma, int mb, long long K, double*
     return ef_fail(EF_ERR_WORKSPACE, "gram work buffer too small");
   cudaStream_t st = (cudaStream_t)stream;
   const bool pipe = (K % 2 == 0) && ((((uintptr_t)A) | ((uintptr_t)B)) % 16 == 0);
+  int tuned = 0;
+  ef::gram_tune_get(ma, mb, &tuned, nullptr);
   const char* kern = getenv("EF_GRAM_KERNEL");
-  const bool tc = kern ? strcmp(kern, "tc") == 0 : gram_use_tc(ma, mb);
+  const bool tc = kern ? strcmp(kern, "tc") == 0 : (tuned ? tuned == 1 : gram_use_tc(ma, mb));
   if (tc && pipe) return ef_gram_tc(A, B, ma, mb, K, G, ef::tc_error_dev(), work, work_bytes, stream);
   int ns = gram_splits(ma, mb, K);
   long long kchunk = (K + ns - 1) / ns;

@@ -25,6 +25,14 @@ struct Op {
   float* eps_n;     // (N) eps / N
   float* eps_raw;   // (N) eps as given (for field outputs)
   float2* tw;       // (G) exp(+2 pi i j / G)
+  // three-pass operator (zplane.cuh) only: eps^-1/N and eps/N per plane z in the
+  // digit-reversed slot order of the plane pass, [z][k1][q][j]
+  float* wperm_inv;
+  float* wperm_eps;
+  // pipeline selection (ef_op_configure): 0 automatic, 3 three-pass, 5 five-pass;
+  // sub-batch workspace cap in bytes (0 = default)
+  int passes;
+  size_t subbatch_bytes;
 };
 
 // Frame at one voxel, computed from the per-axis tables exactly as the reference

@@ -15,6 +15,7 @@
 #include "fft_passes.cuh"
 #include "plan.cuh"
 #include "status.h"
+#include "zplane.cuh"
 
 using namespace ef;
 
@@ -34,6 +35,53 @@ const std::vector<Plan>& plans() {
 const Plan* find_plan(int G) {
   for (const Plan& p : plans()) if (p.G == G) return &p;
   return nullptr;
+}
+
+const std::vector<Plan3>& plans3() {
+  static const std::vector<Plan3> v = [] {
+    std::vector<Plan3> p;
+    add_plans3(p);
+    return p;
+  }();
+  return v;
+}
+
+const Plan3* plan3_of_grid(int G) {
+  for (const Plan3& p : plans3()) if (p.G == G) return &p;
+  return nullptr;
+}
+
+// The three-pass operator serves the grid edges it has a plan for, unless the handle
+// was configured for the five-pass pencil pipeline (ef_op_configure) or, for handles
+// left on automatic, EF_THETA_PASSES=5 is set (comparisons).
+const Plan3* find_plan3(const ef_op* op) {
+  if (op->passes == 5) return nullptr;
+  if (op->passes == 0) {
+    static const bool five = [] {
+      const char* e = std::getenv("EF_THETA_PASSES");
+      return e && std::atoi(e) == 5;
+    }();
+    if (five) return nullptr;
+  }
+  return plan3_of_grid(op->G);
+}
+
+// Plane-pass multiplier in the slot order the plane pass sees between its inverse
+// and forward transforms: slot (row R2*k1 + j, column q) of plane z holds real-space
+// x = k1 + R1*j and y = q/R2 + R1*(q%R2); stored [z][k1][q][j] so that one item's
+// R2 factors are contiguous.
+void permute_plane_table(const std::vector<float>& w, int G, int R1, int R2, std::vector<float>& out) {
+  out.resize(w.size());
+  size_t o = 0;
+  for (int z = 0; z < G; ++z)
+    for (int k1 = 0; k1 < R1; ++k1)
+      for (int q = 0; q < G; ++q) {
+        const int yr = q / R2 + R1 * (q % R2);
+        for (int j = 0; j < R2; ++j) {
+          const int xr = k1 + R1 * j;
+          out[o++] = w[((size_t)xr * G + yr) * G + z];
+        }
+      }
 }
 
 // ---- host-side fp64 frame tables (operator.py:46-59) -----------------------------
@@ -116,18 +164,23 @@ __global__ void finalize_kernel(const double* partials, int tiles, int mode, dou
   }
 }
 
-size_t subbatch_cap_bytes() {
+// Sub-batch workspace cap: the three-pass workspace of one sub-batch should stay in
+// L2 (126 MB) next to the streamed input and output, so it defaults to 64 MB (one
+// vector at 128^3); EF_SUBBATCH_BYTES overrides it for both pipelines.
+size_t subbatch_cap_bytes(const ef_op* op, bool three_pass) {
+  if (op->subbatch_bytes > 0) return op->subbatch_bytes;
   const char* e = std::getenv("EF_SUBBATCH_BYTES");
   if (e) {
     long long v = std::atoll(e);
     if (v > 0) return (size_t)v;
   }
-  return (size_t)96 << 20;
+  return (size_t)(three_pass ? 64 : 96) << 20;
 }
 
 struct Sizes {
   long long N;
-  int tiles;           // pass-E tiles per vector (one partial each)
+  const Plan3* p3;     // three-pass plan, or null for the five-pass pipeline
+  int tiles;           // last-pass tiles per vector (one partial each)
   int tiles_a;         // pass-A tiles per vector
   size_t per_vec;      // E bytes per vector
   size_t per_vec_part; // partial bytes per vector
@@ -136,7 +189,8 @@ struct Sizes {
 Sizes sizes_of(const ef_op* op, const Plan* p) {
   Sizes s;
   s.N = op->N;
-  s.tiles = (op->G * op->G) / p->NRE;
+  s.p3 = find_plan3(op);
+  s.tiles = s.p3 ? (op->G * op->G) / kZT : (op->G * op->G) / p->NRE;
   s.tiles_a = (op->G * op->G) / p->NRA;
   s.per_vec = (size_t)3 * s.N * sizeof(float2);
   s.per_vec_part = ((size_t)s.tiles * 2 * sizeof(double) + 255) / 256 * 256;
@@ -144,7 +198,7 @@ Sizes sizes_of(const ef_op* op, const Plan* p) {
 }
 
 int mb_cap(const ef_op* op, const Sizes& s) {
-  size_t cap = subbatch_cap_bytes() / s.per_vec;
+  size_t cap = subbatch_cap_bytes(op, s.p3 != nullptr) / s.per_vec;
   return cap < 1 ? 1 : (int)(cap > 4096 ? 4096 : cap);
 }
 
@@ -155,7 +209,8 @@ struct Pipe {
   int fin;     // -1 none, else FinMode
 };
 
-// Run the 5-pass pipeline on m vectors in sub-batches.
+// Run the operator pipeline (three-pass where the grid edge has a plan, else the
+// five-pass pencil pipeline) on m vectors in sub-batches.
 int run_pipe(const ef_op* op, const Pipe& pp, const float2* X, float2* out, float2* T0, float2* Y,
              const float2* Z, int m, float s, float c0, float c1, double* fin_out, int fin_ld,
              int fin_k, double fc0, double fc1, void* work, size_t work_bytes, cudaStream_t st) {
@@ -181,30 +236,55 @@ int run_pipe(const ef_op* op, const Pipe& pp, const float2* X, float2* out, floa
   const long long N2 = 2 * op->N;
   for (int v0 = 0; v0 < m; v0 += mb) {
     const int nb = (m - v0) < mb ? (m - v0) : mb;
-    PassArgs a;
-    std::memset(&a, 0, sizeof(a));
-    a.X = X + (long long)v0 * N2;
-    a.E = E;
-    a.out = out ? out + (long long)v0 * N2 : nullptr;
-    a.T0 = T0 ? T0 + (long long)v0 * N2 : nullptr;
-    a.Y = Y ? Y + (long long)v0 * N2 : nullptr;
-    a.Z = Z ? Z + (long long)v0 * N2 : nullptr;
-    a.partials = partials;
-    a.kax = op->kax;
-    a.swap = op->swap;
-    a.w = pp.wmode == W_EPS ? op->eps_n : op->inv_eps;
-    a.tw = op->tw;
-    a.inv_n = 1.0f / (float)op->N;
-    a.kn_floor = op->kn_floor;
-    a.s = s;
-    a.c0 = c0;
-    a.c1 = c1;
-    a.G = G;
-    p->a[pp.build](dim3(sz.tiles_a, nb), smem_a, st, a);
-    p->y[0](dim3(G / NZ, G, 3 * nb), smem_y, st, a);
-    p->c[pp.wmode](dim3(G / NZ, G, 3 * nb), smem_c, st, a);
-    p->y[1](dim3(G / NZ, G, 3 * nb), smem_y, st, a);
-    p->e[pp.epi](dim3(sz.tiles, nb), smem_e, st, a);
+    const long long off = (long long)v0 * N2;
+    if (sz.p3) {
+      const Plan3* q = sz.p3;
+      P3Args a;
+      std::memset(&a, 0, sizeof(a));
+      a.X = X + off;
+      a.W = E;
+      a.out = out ? out + off : nullptr;
+      a.T0 = T0 ? T0 + off : nullptr;
+      a.Y = Y ? Y + off : nullptr;
+      a.Z = Z ? Z + off : nullptr;
+      a.partials = partials;
+      a.kax = op->kax;
+      a.swap = op->swap;
+      a.wperm = pp.wmode == W_EPS ? op->wperm_eps : op->wperm_inv;
+      a.tw = op->tw;
+      a.kn_floor = op->kn_floor;
+      a.s = s;
+      a.c0 = c0;
+      a.c1 = c1;
+      q->zin[pp.build == BUILD_PRECOND ? 1 : 0](dim3(sz.tiles, nb), q->smem_z, st, a);
+      q->plane(dim3(3 * G * nb / q->PL), q->smem_plane, st, a);
+      q->zout[pp.epi](dim3(sz.tiles, nb), q->smem_z, st, a);
+    } else {
+      PassArgs a;
+      std::memset(&a, 0, sizeof(a));
+      a.X = X + off;
+      a.E = E;
+      a.out = out ? out + off : nullptr;
+      a.T0 = T0 ? T0 + off : nullptr;
+      a.Y = Y ? Y + off : nullptr;
+      a.Z = Z ? Z + off : nullptr;
+      a.partials = partials;
+      a.kax = op->kax;
+      a.swap = op->swap;
+      a.w = pp.wmode == W_EPS ? op->eps_n : op->inv_eps;
+      a.tw = op->tw;
+      a.inv_n = 1.0f / (float)op->N;
+      a.kn_floor = op->kn_floor;
+      a.s = s;
+      a.c0 = c0;
+      a.c1 = c1;
+      a.G = G;
+      p->a[pp.build](dim3(sz.tiles_a, nb), smem_a, st, a);
+      p->y[0](dim3(G / NZ, G, 3 * nb), smem_y, st, a);
+      p->c[pp.wmode](dim3(G / NZ, G, 3 * nb), smem_c, st, a);
+      p->y[1](dim3(G / NZ, G, 3 * nb), smem_y, st, a);
+      p->e[pp.epi](dim3(sz.tiles, nb), smem_e, st, a);
+    }
     if (pp.fin >= 0) {
       double* o = (pp.fin == FIN_COUNT_FIRST || pp.fin == FIN_COUNT_STEP) ? fin_out + v0 : fin_out + (long long)v0 * fin_ld;
       ef_count_launches(1);
@@ -328,6 +408,12 @@ int ef_op_create(int grid, double box_size, double kx, double ky, double kz, con
     epsn[i] = eps_host[i] * invN;
   }
   op->eps_mean_inv = acc / (double)N;
+  const Plan3* p3 = plan3_of_grid(G);
+  std::vector<float> pinv, peps;
+  if (p3) {
+    permute_plane_table(inv, G, p3->pl_R1, p3->pl_R2, pinv);
+    permute_plane_table(epsn, G, p3->pl_R1, p3->pl_R2, peps);
+  }
   std::vector<float2> tw(G);
   for (int j = 0; j < G; ++j) {
     double ang = 2.0 * M_PI * (double)j / (double)G;
@@ -346,6 +432,12 @@ int ef_op_create(int grid, double box_size, double kx, double ky, double kz, con
   if (e == cudaSuccess) e = cudaMemcpy(op->eps_n, epsn.data(), (size_t)N * sizeof(float), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(op->eps_raw, eps_host, (size_t)N * sizeof(float), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(op->tw, tw.data(), (size_t)G * sizeof(float2), cudaMemcpyHostToDevice);
+  if (p3) {
+    if (e == cudaSuccess) e = cudaMalloc(&op->wperm_inv, (size_t)N * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&op->wperm_eps, (size_t)N * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpy(op->wperm_inv, pinv.data(), (size_t)N * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(op->wperm_eps, peps.data(), (size_t)N * sizeof(float), cudaMemcpyHostToDevice);
+  }
   if (e != cudaSuccess) {
     ef_op_destroy(op);
     return ef_fail(EF_ERR_CUDA, cudaGetErrorString(e));
@@ -362,8 +454,25 @@ int ef_op_destroy(ef_op* op) {
   cudaFree(op->eps_n);
   cudaFree(op->eps_raw);
   cudaFree(op->tw);
+  cudaFree(op->wperm_inv);
+  cudaFree(op->wperm_eps);
   delete op;
   return EF_OK;
+}
+
+int ef_op_configure(ef_op* op, int passes, size_t subbatch_bytes) {
+  if (!op) return ef_fail(EF_ERR_INVALID, "null operator");
+  if (passes != 0 && passes != 3 && passes != 5) return ef_fail(EF_ERR_INVALID, "passes must be 0, 3 or 5");
+  if (passes == 3 && !plan3_of_grid(op->G))
+    return ef_fail(EF_ERR_UNSUPPORTED, "no three-pass plan for this grid edge");
+  op->passes = passes;
+  op->subbatch_bytes = subbatch_bytes;
+  return EF_OK;
+}
+
+int ef_op_pipeline(const ef_op* op) {
+  if (!op) return 0;
+  return find_plan3(op) ? 3 : 5;
 }
 
 int ef_op_info(const ef_op* op, int* grid, double* kn_floor, double* eps_mean_inv) {

@@ -47,6 +47,10 @@
 #include "tc_common.cuh"
 #include "tmap.h"
 
+namespace ef {
+bool gram_tune_get(int ma, int mb, int* kernel, int* units);
+}
+
 namespace {
 
 using namespace ef::tc;
@@ -476,7 +480,14 @@ bool gc_pack_enabled() {
 // 1.59 against 1.81, at K = 4.2M)
 bool gc_swap(int ma, int mb) { return ma > 32 && mb <= 32 && gc_pack_enabled(); }
 
-GcPlan gc_plan(int ma, int mb, long long K) {
+// units per SM: the autotuner's choice for the caller's (ma, mb), else 2
+int gc_units(int ma, int mb) {
+  int units = 0;
+  ef::gram_tune_get(ma, mb, nullptr, &units);
+  return units > 0 ? units : 2;
+}
+
+GcPlan gc_plan(int ma, int mb, long long K, int units) {
   GcPlan p;
   p.mt = ma <= 32 ? 32 : 64;
   p.pk = (p.mt == 32 && gc_pack_enabled()) ? 2 : 1;
@@ -485,7 +496,7 @@ GcPlan gc_plan(int ma, int mb, long long K) {
   p.njt = (mb + p.nb - 1) / p.nb;
   const long long tiles = (long long)p.nit * p.njt;
   const long long sms = sm_count_dev();
-  long long nk = (2 * sms + tiles - 1) / tiles;               // about two units per SM
+  long long nk = (units * sms + tiles - 1) / tiles;           // about `units` units per SM
   const long long maxk = (K + 2047) / 2048;                   // >= 2048 complex per unit
   if (nk > maxk) nk = maxk;
   if (nk < 1) nk = 1;
@@ -528,7 +539,8 @@ int launch_gc(const GcPlan& p, cudaStream_t st, const float* A, const float* B, 
 
 extern "C" size_t ef_gram_tc_workspace_bytes(int ma, int mb, long long K) {
   if (ma <= 0 || mb <= 0 || K <= 0) return 0;
-  const GcPlan p = gc_swap(ma, mb) ? gc_plan(mb, ma, K) : gc_plan(ma, mb, K);
+  const int u = gc_units(ma, mb);
+  const GcPlan p = gc_swap(ma, mb) ? gc_plan(mb, ma, K, u) : gc_plan(ma, mb, K, u);
   return (size_t)p.nk * p.pk * ma * mb * 2 * sizeof(double) + 512;
 }
 
@@ -541,6 +553,7 @@ extern "C" int ef_gram_tc(const float* A, const float* B, int ma, int mb, long l
   if (!work || work_bytes < ef_gram_tc_workspace_bytes(ma, mb, K))
     return ef_fail(EF_ERR_WORKSPACE, "gram_tc work buffer too small");
   cudaStream_t st = (cudaStream_t)stream;
+  const int units = gc_units(ma, mb);
   const bool swap = gc_swap(ma, mb);
   if (swap) {
     const float* t = A;
@@ -550,7 +563,7 @@ extern "C" int ef_gram_tc(const float* A, const float* B, int ma, int mb, long l
     ma = mb;
     mb = tm;
   }
-  const GcPlan p = gc_plan(ma, mb, K);
+  const GcPlan p = gc_plan(ma, mb, K, units);
   ef_count_launches(2);
   int rc;
   double* part = (double*)work;

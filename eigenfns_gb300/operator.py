@@ -111,6 +111,18 @@ class MaxwellOperator:
             raise ValueError(f"expected a block (m, 2, {G}, {G}, {G}), got {tuple(X.shape)}")
         return X
 
+    def configure(self, passes: int = 0, subbatch_bytes: int = 0) -> None:
+        """Pipeline of the operator applications: passes 0 (automatic), 3 (z / xy-plane / z,
+        grid edges 32, 48, 64, 96, 128) or 5 (pencil passes, every grid edge), and the
+        sub-batch workspace cap in bytes (0 = the library default). Set by the autotuner
+        (eigenfns_gb300.tune)."""
+        call("ef_op_configure", self._h, int(passes), int(subbatch_bytes))
+
+    @property
+    def pipeline(self) -> int:
+        """The pipeline the operator applications use now: 3 or 5."""
+        return int(self._lib.ef_op_pipeline(self._h))
+
     def workspace(self, m: int) -> torch.Tensor:
         nbytes = self._lib.ef_op_workspace_bytes(self._h, int(m))
         return blas.workspace(nbytes, self.device, "op")

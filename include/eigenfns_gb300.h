@@ -62,6 +62,15 @@ int ef_supported_grid(int grid);
 int ef_op_create(int grid, double box_size, double kx, double ky, double kz,
                  const float* eps_host, ef_op** out);
 int ef_op_destroy(ef_op* op);
+/* Pipeline of the operator applications (no counterpart in the reference: the
+ * autotuner's control, eigenfns_gb300/tune.py). passes = 0 automatic (three-pass
+ * z / xy-plane / z pipeline where the grid edge has a plan: 32, 48, 64, 96, 128;
+ * else the five-pass pencil pipeline), 3 (EF_ERR_UNSUPPORTED without a plan) or 5.
+ * subbatch_bytes caps one sub-batch's workspace (0 = default: 64 MB three-pass,
+ * 96 MB five-pass). Applies to ef_op_workspace_bytes and to every later call. */
+int ef_op_configure(ef_op* op, int passes, size_t subbatch_bytes);
+/* the pipeline the handle's operator calls use now: 3 or 5 */
+int ef_op_pipeline(const ef_op* op);
 /* grid_size, kn_floor (operator.py:149-151), eps_mean_inv (:148) */
 int ef_op_info(const ef_op* op, int* grid, double* kn_floor, double* eps_mean_inv);
 /* TransverseBasis.kn (G^3 float32) and .t (2,3,G^3 float32) (operator.py:36-37) */
@@ -142,6 +151,14 @@ int ef_gram(const float* A, const float* B, int ma, int mb, long long K, double*
  * serialised by the caller. Allocates nothing. */
 int ef_gram_noalloc(const float* A, const float* B, int ma, int mb, long long K, double* G,
                     void* stream);
+/* Gram schedule override for one (ma, mb) shape (no counterpart in the reference: set
+ * by the autotuner, eigenfns_gb300/tune.py). kernel 0 = built-in choice, 1 = tensor
+ * cores, 2 = CUDA cores; units_per_sm (0 = default 2) sets how many K-chunks per SM the
+ * tensor-core Gram splits into. Consulted by ef_gram, ef_gram_tc and their workspace
+ * queries; EF_ERR_TOO_LARGE once 256 shapes are registered. */
+int ef_tune_gram(int ma, int mb, int kernel, int units_per_sm);
+/* drops every ef_tune_gram override */
+int ef_tune_reset(void);
 /* reads and clears the sticky device flag the tensor-core rotation sets when one of its
  * bounded waits ran out (never expected; results of that call are not valid).
  * Synchronises the device. */

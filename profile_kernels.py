@@ -8,8 +8,9 @@
     python profile_kernels.py kpm --grid 256 --m 4 --steps 8
     python profile_kernels.py rowstats --ma 32 --mb 32 --grid 128
 
-Each runs 3 warm-up calls and then one timed call (CUDA events on the current
-stream), printing the time; under ncu, skip the warm-up launches with -s.
+Each runs 3 warm-up calls and then --reps timed calls (default 1; CUDA events on
+the current stream), printing the mean time; under ncu, skip the warm-up launches
+with -s.
 Inputs are seeded random blocks and a seeded binary eps grid.
 """
 from __future__ import annotations
@@ -27,16 +28,21 @@ def _op(G: int):
     return MaxwellOperator(eps, 5.0)
 
 
+REPS = 1
+
+
 def _timed(fn, warm: int = 3) -> float:
+    """Mean milliseconds per call over REPS calls after `warm` untimed ones."""
     for _ in range(warm):
         fn()
     torch.cuda.synchronize()
     s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     s.record()
-    fn()
+    for _ in range(REPS):
+        fn()
     e.record()
     torch.cuda.synchronize()
-    return s.elapsed_time(e)
+    return s.elapsed_time(e) / REPS
 
 
 def main(argv=None) -> None:
@@ -48,7 +54,10 @@ def main(argv=None) -> None:
     ap.add_argument("--ma", type=int, default=32)
     ap.add_argument("--mb", type=int, default=32)
     ap.add_argument("--steps", type=int, default=4)
+    ap.add_argument("--reps", type=int, default=1, help="timed calls (mean reported)")
     a = ap.parse_args(argv)
+    global REPS
+    REPS = max(1, a.reps)
     g = torch.Generator(device="cuda").manual_seed(1)
     G = a.grid
     if a.kernel in ("theta", "precond", "cheb", "kpm"):
@@ -66,7 +75,10 @@ def main(argv=None) -> None:
         else:
             from eigenfns_gb300.kpm import kpm_moments
             ms = _timed(lambda: kpm_moments(op, 4.0e4, 2 * a.steps, a.m, Z=X))
-        print(f"{a.kernel} grid {G} m {a.m}: {ms:.3f} ms")
+        us = 1e3 * ms / a.m
+        gbs = (32.0 * G ** 3 * a.m + 4.0 * G ** 3) / (ms * 1e-3) / 1e9
+        print(f"{a.kernel} grid {G} m {a.m}: {ms:.3f} ms  ({us:.1f} us/vector, "
+              f"{gbs:.0f} GB/s of compulsory operator bytes)")
     else:
         from eigenfns_gb300 import blas
         K = 2 * G ** 3

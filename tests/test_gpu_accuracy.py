@@ -41,3 +41,36 @@ def test_structure_fixture_rasterizes_identically():
     d = np.load(GOLD / "fp64_n64_g32_gamma.npz")
     net = generate_network(int(d["nodes"]), int(d["seed"]))
     assert np.array_equal(rasterize(net, int(d["grid"]), sub=4), d["eps"])
+
+
+HEADLINE = GOLD / "fp64_n1000_g128_gamma.npz"
+
+
+@pytest.mark.parametrize("mode", ["mixed", "fp32"])
+def test_headline_workload_eigenvalues_within_1e6_of_fp64(mode):
+    """The N=1000 rod network at 128^3, Γ, block 32 / guard 8, lock at 1e-4: every band
+    the complex128 run of the same method holds (tests/golden/make_fp64_reference.py)
+    within 1e-6 relative, with the block algebra on the tensor cores (3xTF32, "mixed")
+    and on the CUDA cores in plain fp32 ("fp32")."""
+    from eigenfns_gb300 import blas
+    from eigenfns_gb300.operator import MaxwellOperator
+    from eigenfns_gb300.solver import lobpcg_blocks
+    d = np.load(HEADLINE)
+    ref = d["vals"]
+    op = MaxwellOperator(d["eps"], float(d["box"]), k_frac=tuple(d["k"]))
+    with blas.precision(mode):
+        vals, _, st = lobpcg_blocks(op, len(ref), m=int(d["m"]), guard=int(d["guard"]), tol=1e-4,
+                                    maxit=400, seed=0, verbose=False)
+    err = np.abs(vals - ref) / ref
+    print(f"{mode}: {len(ref)} bands, max rel err {err.max():.2e}, median {np.median(err):.2e}")
+    assert err.max() <= 1e-6, err.max()
+
+
+def test_headline_structure_rasterizes_identically():
+    """The GPU rasterizer reproduces the 128^3 eps grid the headline fixture was solved on."""
+    import hashlib
+    from eigenfns_gb300.structure import generate_network, rasterize
+    d = np.load(HEADLINE)
+    net = generate_network(int(d["nodes"]), int(d["seed"]))
+    eps = rasterize(net, int(d["grid"]), sub=4)
+    assert hashlib.sha256(np.ascontiguousarray(eps).tobytes()).hexdigest() == str(d["eps_sha256"])
