@@ -93,14 +93,25 @@ def _theta(op, X, stats, out=None):
 
 
 def _ortho_inplace(X: torch.Tensor, passes: int = 2, drop: float = _SVQB_DROP) -> None:
-    """SVQB on a contiguous block slot, written back into the slot."""
+    """SVQB on a contiguous block slot, written back into the slot.
+
+    The first pass is the reference's SVQB (host fp64 eigh with the 1e-5 drop). After it
+    every row is unit or zero, so the second pass is a well-conditioned re-orthonormalisation
+    within the same span: it runs as a device fp64 Cholesky-QR (ef_cholqr_f64, zero rows
+    stay zero), which saves a device-to-host round trip and a host eigh; the Rayleigh-Ritz
+    step that follows depends only on the span."""
+    from . import dense
     m = int(X.shape[0])
-    for _ in range(passes):
-        C, _ = svqb_coeffs(gram(X, X).cpu().numpy(), drop)
-        if m <= 32:
-            rotate(C.astype(np.complex64), X, X)
+    for p in range(passes):
+        if p > 0 and m <= dense.MAX_N:
+            C, _ = dense.cholqr_coeffs(gram(X, X), tol=drop)
         else:
-            X.copy_(rotate(C.astype(np.complex64), X))
+            C, _ = svqb_coeffs(gram(X, X).cpu().numpy(), drop)
+            C = C.astype(np.complex64)
+        if m <= 32:
+            rotate(C, X, X)
+        else:
+            X.copy_(rotate(C, X))
 
 
 def _normalize_rows(X: torch.Tensor, floor: float) -> None:
@@ -146,8 +157,13 @@ def lobpcg_blocks(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
                   maxit: int = 400, seed: int = 0, precond_shift: str = "median",
                   verbose: bool = True, log_every: int = 0, initial_locked=None,
                   initial_vals=None, on_block=None, locked_storage: str = "auto",
-                  theta_chunk: int = 0, normalize_rq: bool = True, deflate_chunk: int | None = None):
+                  theta_chunk: int = 0, normalize_rq: bool = True, deflate_chunk: int | None = None,
+                  autotune: bool | None = None):
     """Bottom-up deflated block LOBPCG. Returns (eigenvalues, locked_vectors, stats).
+
+    `autotune` (default: on when EF_AUTOTUNE=1) times the operator pipeline and the
+    Gram schedules of this block size once on the running GPU before the solve and
+    reuses the cached choice afterwards (eigenfns_gb300.tune).
 
     Working set: two (3m, 2, G, G, G) slabs holding the blocks as [P; X; W] (the
     Rayleigh-Ritz basis is contiguous, so its Gram is one call and the Ritz
@@ -157,6 +173,9 @@ def lobpcg_blocks(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
     """
     G = op.grid_size
     dev = op.device
+    from . import tune
+    if tune.enabled(autotune) and hasattr(op, "configure"):
+        tune.autotune(op, m)
     vshape = op.vec_shape(1)[1:]
     cap = int(np.ceil(nev / max(m - guard, 1))) * (m - guard) + m
     n_init = 0 if initial_locked is None else int(initial_locked.shape[0])

