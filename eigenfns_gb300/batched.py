@@ -1,0 +1,130 @@
+"""Many eigensolves in lock step on one GPU (the batched path).
+
+Each solve is the deflated block LOBPCG of eigenfns_gb300.solver written as a step
+generator (solver.lobpcg_steps): the algorithm runs until it needs device data on the
+host (residual norms, an SVQB Gram, the Rayleigh-Ritz matrix) and yields those device
+tensors. The driver here advances every active solve to its next such point, which
+queues that solve's kernels on the shared stream, then copies all the requested
+tensors to pinned host memory and synchronizes once for the whole batch, and resumes
+each solve with its data. Per step the host therefore waits once for all instances
+instead of once per instance, the GPU runs the instances' kernels back to back, and
+each solve's small host work (fp64 eigh) overlaps the device work queued by the solves
+after it. Solves may join and leave between steps (continuous batching, see
+eigenfns_gb300.serve). A solve's kernels and their order are exactly those of the solve
+run alone, so its results are identical alone and in the batch.
+
+Reference: the per-instance algorithm is eigenfns/solver.py:136-382; the reference has
+no batched path (its multi-instance runs are separate processes, e.g.
+scripts/exp/chain_i6resume.sh).
+"""
+from __future__ import annotations
+
+import torch
+
+from . import blas
+from .solver import lobpcg_steps
+
+
+def _pinned_copy(t: torch.Tensor) -> torch.Tensor:
+    h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+    h.copy_(t, non_blocking=True)
+    return h
+
+
+def _request_to_host(req):
+    if isinstance(req, tuple):
+        return tuple(_pinned_copy(t) for t in req)
+    return _pinned_copy(req)
+
+
+def _numpy(h):
+    if isinstance(h, tuple):
+        return tuple(x.numpy() for x in h)
+    return h.numpy()
+
+
+class BatchedSolves:
+    """Lock-step driver of step generators that share one CUDA stream."""
+
+    def __init__(self):
+        self._active: dict = {}     # key -> (generator, pending request)
+        self.steps = 0
+
+    def __len__(self) -> int:
+        return len(self._active)
+
+    def keys(self):
+        return list(self._active)
+
+    def add(self, key, gen) -> dict:
+        """Start a solve (runs it up to its first host read). Returns {key: result} if it
+        finished without reading anything (never for LOBPCG)."""
+        try:
+            self._active[key] = (gen, next(gen))
+        except StopIteration as stop:
+            return {key: stop.value}
+        return {}
+
+    def step(self) -> dict:
+        """One shared host transfer and one resume of every active solve; returns the
+        solves that finished in this step as {key: result or the exception raised}."""
+        if not self._active:
+            return {}
+        hosts = {k: _request_to_host(req) for k, (_, req) in self._active.items()}
+        torch.cuda.current_stream().synchronize()
+        self.steps += 1
+        if blas.tc_error():
+            # a tensor-core pipeline wait ran out in some solve since the last step: every
+            # solve in flight may hold invalid data, so all of them fail
+            err = RuntimeError("a tensor-core kernel timed out waiting on its pipeline; results invalid")
+            done = {k: err for k in self._active}
+            for g, _ in self._active.values():
+                g.close()
+            self._active.clear()
+            return done
+        finished = {}
+        for k in list(self._active):
+            gen, _ = self._active[k]
+            try:
+                self._active[k] = (gen, gen.send(_numpy(hosts[k])))
+            except StopIteration as stop:
+                finished[k] = stop.value
+                del self._active[k]
+            except Exception as exc:            # surfaced to the caller per solve
+                finished[k] = exc
+                del self._active[k]
+        return finished
+
+    def run(self) -> dict:
+        """Step until every solve has finished; returns {key: result}."""
+        out = {}
+        while self._active:
+            out.update(self.step())
+        return out
+
+
+def lobpcg_batched(ops, nevs, m: int = 32, guard: int = 8, tol: float = 1e-4, maxit: int = 400,
+                   seeds=None, **kw) -> list:
+    """Solve several operators' lowest eigenpairs in lock step.
+
+    `ops` are MaxwellOperators (any mix of grids and k-points), `nevs` the bands wanted
+    from each (an int applies to all); `m`/`guard` may also be per-instance lists.
+    Returns [(eigenvalues, locked vectors, SolveStats)] in the order of `ops`, each equal
+    to lobpcg_blocks(op, nev, ...) run alone; raises the first failure after the batch.
+    """
+    n = len(ops)
+    per = lambda v: list(v) if isinstance(v, (list, tuple)) else [v] * n
+    nevs, ms, guards = per(nevs), per(m), per(guard)
+    seeds = per(0 if seeds is None else seeds)
+    drv = BatchedSolves()
+    out = {}
+    for i, op in enumerate(ops):
+        out.update(drv.add(i, lobpcg_steps(op, nevs[i], m=ms[i], guard=guards[i], tol=tol,
+                                           maxit=maxit, seed=seeds[i], verbose=False,
+                                           check_tc=False, **kw)))
+    out.update(drv.run())
+    res = [out[i] for i in range(n)]
+    for r in res:
+        if isinstance(r, Exception):
+            raise r
+    return res

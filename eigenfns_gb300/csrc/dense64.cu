@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(kDenseThreads) jacobi_kernel(const double2* __
     }
     off = block_sum_d(off, red);
     tot = block_sum_d(tot, red);
-    if (!(off > 1e-30 * tot)) break;       // uniform across the block
+    if (!(off > 1e-26 * tot)) break;       // uniform across the block; ~1e-13 relative
     for (int r = 0; r < ne - 1; ++r) {
       for (int k = threadIdx.x; k < ne / 2; k += blockDim.x) {
         int p = rr_index(k, r, ne), q = rr_index(ne - 1 - k, r, ne);

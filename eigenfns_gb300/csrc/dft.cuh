@@ -47,16 +47,47 @@ __host__ __device__ constexpr double ce_sinpi(long num, long den) {
 }
 
 // ---- complex helpers -------------------------------------------------------------
+// With EF_F32X2 (the default) additions, subtractions and scalings use the paired
+// fp32 instructions of sm_100 and later (one instruction for the real and imaginary
+// parts; IEEE round-to-nearest per component, so results equal the scalar forms:
+// a - b is computed as b * (-1) + a, whose product is exact).
+#ifndef EF_F32X2
+#define EF_F32X2 1
+#endif
+#if EF_F32X2
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+  return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+}
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return __fmul2_rn(a, make_float2(s, s)); }
+// a + (sx * b.y, sy * b.x): the building block of a +/- i b
+__device__ __forceinline__ float2 cadd_swapped(float2 a, float2 b, float sx, float sy) {
+  return __ffma2_rn(make_float2(b.y, b.x), make_float2(sx, sy), a);
+}
+#else
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__device__ __forceinline__ float2 cadd_swapped(float2 a, float2 b, float sx, float sy) {
+  return make_float2(fmaf(sx, b.y, a.x), fmaf(sy, b.x, a.y));
+}
+#endif
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
-__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 // multiply by DIR*i  (i.e. +i for DIR=+1, -i for DIR=-1)
 template <int DIR>
 __device__ __forceinline__ float2 mul_dir_i(float2 a) {
   return DIR > 0 ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+// a + DIR*i*b and a - DIR*i*b
+template <int DIR>
+__device__ __forceinline__ float2 cadd_i(float2 a, float2 b) {
+  return DIR > 0 ? cadd_swapped(a, b, -1.f, 1.f) : cadd_swapped(a, b, 1.f, -1.f);
+}
+template <int DIR>
+__device__ __forceinline__ float2 csub_i(float2 a, float2 b) {
+  return DIR > 0 ? cadd_swapped(a, b, 1.f, -1.f) : cadd_swapped(a, b, -1.f, 1.f);
 }
 
 // twiddle exp(DIR * 2 pi i * num / den) as a compile-time constant
@@ -93,12 +124,11 @@ struct DFT<3, DIR> {
     constexpr float h = 0.8660254037844386f;  // sqrt(3)/2
     float2 x0 = v[0], x1 = v[1], x2 = v[2];
     float2 t1 = cadd(x1, x2);
-    float2 d = csub(x1, x2);
+    float2 d = cscale(csub(x1, x2), h);
     float2 m = make_float2(x0.x - 0.5f * t1.x, x0.y - 0.5f * t1.y);
-    float2 r = mul_dir_i<DIR>(cscale(d, h));
     v[0] = cadd(x0, t1);
-    v[1] = cadd(m, r);
-    v[2] = csub(m, r);
+    v[1] = cadd_i<DIR>(m, d);
+    v[2] = csub_i<DIR>(m, d);
   }
 };
 
@@ -107,11 +137,11 @@ struct DFT<4, DIR> {
   template <typename A>
   __device__ __forceinline__ static void run(A& v) {
     float2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
-    float2 c = cadd(v[1], v[3]), d = mul_dir_i<DIR>(csub(v[1], v[3]));
+    float2 c = cadd(v[1], v[3]), e = csub(v[1], v[3]);
     v[0] = cadd(a, c);
     v[2] = csub(a, c);
-    v[1] = cadd(b, d);
-    v[3] = csub(b, d);
+    v[1] = cadd_i<DIR>(b, e);
+    v[3] = csub_i<DIR>(b, e);
   }
 };
 
@@ -183,7 +213,17 @@ struct DFT {
     if constexpr (I < N) {
       constexpr int A = Split<N>::A;
       constexpr int n2 = I / A, k1 = I % A;
-      if constexpr (n2 * k1 != 0) y[I] = cmul(y[I], ctw<DIR, long(n2 * k1), long(N)>());
+      constexpr int p = n2 * k1;
+      if constexpr (p != 0) {
+        if constexpr ((4 * p) % N == 0) {          // exact quarter turns: (DIR i)^q
+          constexpr int q = (4 * p / N) % 4;
+          if constexpr (q == 1) y[I] = mul_dir_i<DIR>(y[I]);
+          else if constexpr (q == 2) y[I] = make_float2(-y[I].x, -y[I].y);
+          else if constexpr (q == 3) y[I] = mul_dir_i<-DIR>(y[I]);
+        } else {
+          y[I] = cmul(y[I], ctw<DIR, long(p), long(N)>());
+        }
+      }
       twiddle_all<I + 1>(y);
     }
   }

@@ -42,7 +42,40 @@
 namespace ef {
 
 constexpr int kZT = 16;      // z-pass tile: consecutive ky rows at one kx
-constexpr int kZThreads = 128;
+constexpr int kZThreads = 256;
+constexpr int kZMinBlocks = 3;
+
+// Work items are distributed over the threads in compile-time rounds, so that a
+// thread's loads of all its items can be issued together.
+#define EF_ITEMS(ITEMS, NT, ...)                                                           \
+  _Pragma("unroll") for (int round_ = 0; round_ < ((ITEMS) + (NT) - 1) / (NT); ++round_) { \
+    const int it = (int)threadIdx.x + round_ * (NT);                                       \
+    if ((ITEMS) % (NT) == 0 || it < (ITEMS)) { __VA_ARGS__ }                               \
+  }
+
+// Per-tile frame inputs staged in shared memory by the z passes: K_z for every z,
+// K_y for the tile's rows, and the reference-axis switch bit of each (row, z).
+template <int G>
+struct ZFrame {
+  float kz[G];
+  float ky[kZT];
+  uint8_t sw[kZT * G];
+  float kx;
+  __device__ __forceinline__ void load(const float* __restrict__ kax, const uint32_t* __restrict__ swap,
+                                       int kx_, int ky0) {
+    for (int i = threadIdx.x; i < G; i += blockDim.x) kz[i] = kax[2 * G + i];
+    for (int i = threadIdx.x; i < kZT; i += blockDim.x) ky[i] = kax[G + ky0 + i];
+    const unsigned b0 = ((unsigned)kx_ * G + ky0) * G;   // the tile's rows are consecutive
+    for (int i = threadIdx.x; i < kZT * G; i += blockDim.x) {
+      const unsigned b = b0 + i;
+      sw[i] = (uint8_t)((__ldg(swap + (b >> 5)) >> (b & 31)) & 1u);
+    }
+    if (threadIdx.x == 0) kx = kax[kx_];
+  }
+  __device__ __forceinline__ Frame at(int r, int z) const {
+    return make_frame(kx, ky[r], kz[z], sw[r * G + z] != 0);
+  }
+};
 
 struct P3Args {
   const float2* X;     // Z-in input block (m,2,N) at the sub-batch start; T1 for recurrences
@@ -91,22 +124,23 @@ __device__ __forceinline__ void sts_row(float2* p, const float2 (&u)[R]) {
 // Z-in: z-pencils, inverse, with the transverse -> Cartesian build.
 // grid (G*G/16, mb); X points at the sub-batch's first vector.
 template <int R1, int R2, int BUILD>
-__global__ void __launch_bounds__(kZThreads) zin_kernel(P3Args a) {
-  constexpr int G = R1 * R2, T = kZT, ZRS = G + 2;
+__global__ void __launch_bounds__(kZThreads, kZMinBlocks) zin_kernel(P3Args a) {
+  constexpr int G = R1 * R2, T = kZT, ZRS = G + 2, NT = kZThreads;
   static_assert(R2 % 2 == 0 && G % T == 0, "z-in split");
   __shared__ float2 tw_s[G];
+  __shared__ ZFrame<G> fr;
   extern __shared__ float4 zin_smem[];
   float2* buf = reinterpret_cast<float2*>(zin_smem);   // [3][T][ZRS]
-  for (int i = threadIdx.x; i < G; i += kZThreads) tw_s[i] = a.tw[i];
-  __syncthreads();
-  const long long N = (long long)G * G * G, GG = (long long)G * G;
+  constexpr unsigned N = (unsigned)G * G * G, GG = (unsigned)G * G;
   const int kx = blockIdx.x / (G / T), ky0 = (blockIdx.x % (G / T)) * T;
-  const int v = blockIdx.y;
-  const float2* Xa = a.X + (long long)v * 2 * N;
+  for (int i = threadIdx.x; i < G; i += NT) tw_s[i] = a.tw[i];
+  fr.load(a.kax, a.swap, kx, ky0);
+  __syncthreads();
+  const float2* Xa = a.X + (size_t)blockIdx.y * 2 * N;
   const float2* Xb = Xa + N;
-  for (int it = threadIdx.x; it < T * R2; it += kZThreads) {
-    const int t2 = it % R2, r = it / R2, ky = ky0 + r;
-    const long long rb = ((long long)kx * G + ky) * G;
+  EF_ITEMS(T * R2, NT, {
+    const int t2 = it % R2, r = it / R2;
+    const unsigned rb = ((unsigned)kx * G + ky0 + r) * G;
     float2 av[R1], bv[R1];
 #pragma unroll
     for (int n1 = 0; n1 < R1; ++n1) {
@@ -116,7 +150,7 @@ __global__ void __launch_bounds__(kZThreads) zin_kernel(P3Args a) {
     float2 cx[R1], cy[R1], cz[R1];
 #pragma unroll
     for (int n1 = 0; n1 < R1; ++n1) {
-      const Frame f = frame_at(a.kax, a.swap, G, kx, ky, t2 + R2 * n1);
+      const Frame f = fr.at(r, t2 + R2 * n1);
       float2 c1, c2;
       if (BUILD == BUILD_THETA) {           // c1 = -i kn b, c2 = i kn a
         c1 = make_float2(f.kn * bv[n1].y, -f.kn * bv[n1].x);
@@ -145,18 +179,18 @@ __global__ void __launch_bounds__(kZThreads) zin_kernel(P3Args a) {
       b0[1 * T * ZRS + R2 * k1] = y;
       b0[2 * T * ZRS + R2 * k1] = z;
     }
-  }
+  })
   __syncthreads();
-  float2* Wv = a.W + (long long)v * 3 * N;
-  for (int it = threadIdx.x; it < 3 * T * R1; it += kZThreads) {
+  float2* Wv = a.W + (size_t)blockIdx.y * 3 * N;
+  EF_ITEMS(3 * T * R1, NT, {
     const int r = it % T, k1 = (it / T) % R1, c = it / (T * R1);
     float2 u[R2];
     lds_row<R2>(buf + (c * T + r) * ZRS + R2 * k1, u);
     DFT<R2, +1>::run(u);
-    float2* dst = Wv + (long long)c * N + (long long)kx * G + ky0 + r;
+    float2* dst = Wv + (size_t)c * N + (unsigned)kx * G + ky0 + r;
 #pragma unroll
-    for (int k2 = 0; k2 < R2; ++k2) dst[(long long)(k1 + R1 * k2) * GG] = u[k2];
-  }
+    for (int k2 = 0; k2 < R2; ++k2) dst[(unsigned)(k1 + R1 * k2) * GG] = u[k2];
+  })
 }
 
 // ---------------------------------------------------------------------------------
@@ -165,40 +199,51 @@ __global__ void __launch_bounds__(kZThreads) zin_kernel(P3Args a) {
 template <int R1, int R2, int PL, int NT>
 __global__ void __launch_bounds__(NT) plane_kernel(P3Args a) {
   constexpr int G = R1 * R2, RS = G + 2, PSZ = G * RS, NROW = PL * G;
-  static_assert(R2 % 2 == 0, "plane split");
+  static_assert(R2 % 4 == 0, "plane split");
   __shared__ float2 tw_s[G];
   extern __shared__ float4 plane_smem[];
   float2* S = reinterpret_cast<float2*>(plane_smem);  // [PL][G][RS]
   for (int i = threadIdx.x; i < G; i += NT) tw_s[i] = a.tw[i];
   __syncthreads();
-  const long long GG = (long long)G * G;
-  const long long P0 = (long long)blockIdx.x * PL;
+  constexpr unsigned GG = (unsigned)G * G;
+  const size_t P0 = (size_t)blockIdx.x * PL;
   float2* Wp = a.W + P0 * GG;
 
   // y inverse, step A: global -> shared
-  for (int it = threadIdx.x; it < NROW * R2; it += NT) {
+  EF_ITEMS(NROW * R2, NT, {
     const int t2 = it % R2, row = it / R2;
     float2 u[R1];
 #pragma unroll
-    for (int n1 = 0; n1 < R1; ++n1) u[n1] = Wp[(long long)row * G + t2 + R2 * n1];
+    for (int n1 = 0; n1 < R1; ++n1) u[n1] = Wp[(unsigned)row * G + t2 + R2 * n1];
     DFT<R1, +1>::run(u);
     float2* d = S + row * RS + t2;
 #pragma unroll
     for (int k1 = 0; k1 < R1; ++k1) d[R2 * k1] = (k1 && t2) ? cmul(u[k1], twid<+1>(tw_s, t2 * k1)) : u[k1];
-  }
+  })
   __syncthreads();
   // y inverse, step B
-  for (int it = threadIdx.x; it < NROW * R1; it += NT) {
+  EF_ITEMS(NROW * R1, NT, {
     const int row = it % NROW, k1 = it / NROW;
     float2 u[R2];
     float2* p = S + row * RS + R2 * k1;
     lds_row<R2>(p, u);
     DFT<R2, +1>::run(u);
     sts_row<R2>(p, u);
-  }
+  })
   __syncthreads();
+  // the pointwise factors of the x step B items, fetched now so that their latency
+  // overlaps the x step A
+  constexpr int XB_ROUNDS = (PL * G * R1 + NT - 1) / NT;
+  float4 wpre[XB_ROUNDS][R2 / 4];
+  EF_ITEMS(PL * G * R1, NT, {
+    const int q = it % G, k1 = (it / G) % R1, pl = it / (G * R1);
+    const unsigned z = (unsigned)((P0 + pl) % G);
+    const float4* wq = reinterpret_cast<const float4*>(a.wperm + z * GG + ((unsigned)k1 * G + q) * R2);
+#pragma unroll
+    for (int j = 0; j < R2 / 4; ++j) wpre[round_][j] = __ldg(wq + j);
+  })
   // x inverse, step A
-  for (int it = threadIdx.x; it < PL * G * R2; it += NT) {
+  EF_ITEMS(PL * G * R2, NT, {
     const int q = it % G, t2 = (it / G) % R2, pl = it / (G * R2);
     float2* col = S + pl * PSZ + q;
     float2 u[R1];
@@ -208,33 +253,31 @@ __global__ void __launch_bounds__(NT) plane_kernel(P3Args a) {
 #pragma unroll
     for (int k1 = 0; k1 < R1; ++k1)
       col[(t2 + R2 * k1) * RS] = (k1 && t2) ? cmul(u[k1], twid<+1>(tw_s, t2 * k1)) : u[k1];
-  }
+  })
   __syncthreads();
   // x inverse step B, pointwise multiply, x forward step B^T
-  for (int it = threadIdx.x; it < PL * G * R1; it += NT) {
+  EF_ITEMS(PL * G * R1, NT, {
     const int q = it % G, k1 = (it / G) % R1, pl = it / (G * R1);
-    const int z = (int)((P0 + pl) % G);
     float2* col = S + pl * PSZ + (R2 * k1) * RS + q;
+    const float4* w4 = wpre[round_];
     float2 u[R2];
 #pragma unroll
     for (int j = 0; j < R2; ++j) u[j] = col[j * RS];
     DFT<R2, +1>::run(u);
-    const float4* wq = reinterpret_cast<const float4*>(a.wperm + (long long)z * GG + ((long long)k1 * G + q) * R2);
 #pragma unroll
     for (int j = 0; j < R2 / 4; ++j) {
-      const float4 w = __ldg(wq + j);
-      u[4 * j + 0] = cscale(u[4 * j + 0], w.x);
-      u[4 * j + 1] = cscale(u[4 * j + 1], w.y);
-      u[4 * j + 2] = cscale(u[4 * j + 2], w.z);
-      u[4 * j + 3] = cscale(u[4 * j + 3], w.w);
+      u[4 * j + 0] = cscale(u[4 * j + 0], w4[j].x);
+      u[4 * j + 1] = cscale(u[4 * j + 1], w4[j].y);
+      u[4 * j + 2] = cscale(u[4 * j + 2], w4[j].z);
+      u[4 * j + 3] = cscale(u[4 * j + 3], w4[j].w);
     }
     DFT<R2, -1>::run(u);
 #pragma unroll
     for (int j = 0; j < R2; ++j) col[j * RS] = u[j];
-  }
+  })
   __syncthreads();
   // x forward, step A^T: twiddle, DFT_R1, natural kx order
-  for (int it = threadIdx.x; it < PL * G * R2; it += NT) {
+  EF_ITEMS(PL * G * R2, NT, {
     const int q = it % G, t2 = (it / G) % R2, pl = it / (G * R2);
     float2* col = S + pl * PSZ + q;
     float2 u[R1];
@@ -246,29 +289,29 @@ __global__ void __launch_bounds__(NT) plane_kernel(P3Args a) {
     DFT<R1, -1>::run(u);
 #pragma unroll
     for (int n1 = 0; n1 < R1; ++n1) col[(t2 + R2 * n1) * RS] = u[n1];
-  }
+  })
   __syncthreads();
   // y forward, step B^T
-  for (int it = threadIdx.x; it < NROW * R1; it += NT) {
+  EF_ITEMS(NROW * R1, NT, {
     const int row = it % NROW, k1 = it / NROW;
     float2 u[R2];
     float2* p = S + row * RS + R2 * k1;
     lds_row<R2>(p, u);
     DFT<R2, -1>::run(u);
     sts_row<R2>(p, u);
-  }
+  })
   __syncthreads();
   // y forward, step A^T: shared -> global, natural ky order
-  for (int it = threadIdx.x; it < NROW * R2; it += NT) {
+  EF_ITEMS(NROW * R2, NT, {
     const int t2 = it % R2, row = it / R2;
-    const float2* s = S + row * RS + t2;
+    const float2* sp = S + row * RS + t2;
     float2 u[R1];
 #pragma unroll
-    for (int k1 = 0; k1 < R1; ++k1) u[k1] = (k1 && t2) ? cmul(s[R2 * k1], twid<-1>(tw_s, t2 * k1)) : s[R2 * k1];
+    for (int k1 = 0; k1 < R1; ++k1) u[k1] = (k1 && t2) ? cmul(sp[R2 * k1], twid<-1>(tw_s, t2 * k1)) : sp[R2 * k1];
     DFT<R1, -1>::run(u);
 #pragma unroll
-    for (int n1 = 0; n1 < R1; ++n1) Wp[(long long)row * G + t2 + R2 * n1] = u[n1];
-  }
+    for (int n1 = 0; n1 < R1; ++n1) Wp[(unsigned)row * G + t2 + R2 * n1] = u[n1];
+  })
 }
 
 // ---------------------------------------------------------------------------------
@@ -286,36 +329,37 @@ __device__ __forceinline__ int zswz(int pos) {
 
 // grid (G*G/16, mb); per-vector pointers (out, X, T0, Y, Z) at the sub-batch start.
 template <int R1, int R2, int EPI>
-__global__ void __launch_bounds__(kZThreads) zout_kernel(P3Args a) {
-  constexpr int G = R1 * R2, T = kZT, ZRS = G + 2, CPB = R2 / 2;
+__global__ void __launch_bounds__(kZThreads, kZMinBlocks) zout_kernel(P3Args a) {
+  constexpr int G = R1 * R2, T = kZT, ZRS = G + 2, CPB = R2 / 2, NT = kZThreads;
   static_assert(R2 == 4 || R2 == 8 || R2 == 16, "z-out split: R2 a power of two 4..16");
   static_assert(R1 >= 8 && G % T == 0, "z-out split: R1 >= 8");
   __shared__ float2 tw_s[G];
-  __shared__ double red[kZThreads / 32];
+  __shared__ double red[NT / 32];
+  __shared__ ZFrame<G> fr;
   extern __shared__ float4 zout_smem[];
   float2* buf = reinterpret_cast<float2*>(zout_smem);   // [3][T][ZRS]
-  for (int i = threadIdx.x; i < G; i += kZThreads) tw_s[i] = a.tw[i];
-  __syncthreads();
-  const long long N = (long long)G * G * G, GG = (long long)G * G;
+  constexpr unsigned N = (unsigned)G * G * G, GG = (unsigned)G * G;
   const int kx = blockIdx.x / (G / T), ky0 = (blockIdx.x % (G / T)) * T;
-  const int v = blockIdx.y;
-  const float2* Wv = a.W + (long long)v * 3 * N;
-  for (int it = threadIdx.x; it < 3 * T * R2; it += kZThreads) {
+  for (int i = threadIdx.x; i < G; i += NT) tw_s[i] = a.tw[i];
+  fr.load(a.kax, a.swap, kx, ky0);
+  __syncthreads();
+  const float2* Wv = a.W + (size_t)blockIdx.y * 3 * N;
+  EF_ITEMS(3 * T * R2, NT, {
     const int r = it % T, t2 = (it / T) % R2, c = it / (T * R2);
-    const float2* src = Wv + (long long)c * N + (long long)kx * G + ky0 + r;
+    const float2* src = Wv + (size_t)c * N + (unsigned)kx * G + ky0 + r + (unsigned)t2 * GG;
     float2 u[R1];
 #pragma unroll
-    for (int n1 = 0; n1 < R1; ++n1) u[n1] = src[(long long)(t2 + R2 * n1) * GG];
+    for (int n1 = 0; n1 < R1; ++n1) u[n1] = src[(unsigned)(R2 * n1) * GG];
     DFT<R1, -1>::run(u);
     float2* d = buf + (c * T + r) * ZRS;
 #pragma unroll
     for (int k1 = 0; k1 < R1; ++k1)
       d[zswz<CPB>(t2 + R2 * k1)] = (k1 && t2) ? cmul(u[k1], twid<-1>(tw_s, t2 * k1)) : u[k1];
-  }
+  })
   __syncthreads();
-  const long long vo = (long long)v * 2 * N;
+  const size_t vo = (size_t)blockIdx.y * 2 * N;
   double acc0 = 0.0, acc1 = 0.0;
-  for (int it = threadIdx.x; it < T * R1; it += kZThreads) {
+  EF_ITEMS(T * R1, NT, {
     const int k1 = it % R1, r = it / R1, ky = ky0 + r;
     float2 dx[R2], dy[R2], dz[R2];
 #pragma unroll
@@ -332,12 +376,12 @@ __global__ void __launch_bounds__(kZThreads) zout_kernel(P3Args a) {
     DFT<R2, -1>::run(dy);
     DFT<R2, -1>::run(dz);
     float f0 = 0.f, f1acc = 0.f;
-    const long long rowo = ((long long)kx * G + ky) * G;
+    const unsigned rowo = ((unsigned)kx * G + ky) * G;
 #pragma unroll
     for (int k2 = 0; k2 < R2; ++k2) {
       const int kz = k1 + R1 * k2;
-      const long long idx = rowo + kz;
-      const Frame f = frame_at(a.kax, a.swap, G, kx, ky, kz);
+      const size_t idx = rowo + kz;
+      const Frame f = fr.at(r, kz);
       const float2 p1 = make_float2(f.t1x * dx[k2].x + f.t1y * dy[k2].x + f.t1z * dz[k2].x,
                                     f.t1x * dx[k2].y + f.t1y * dy[k2].y + f.t1z * dz[k2].y);
       const float2 p2 = make_float2(f.t2x * dx[k2].x + f.t2y * dy[k2].x + f.t2z * dz[k2].x,
@@ -390,12 +434,12 @@ __global__ void __launch_bounds__(kZThreads) zout_kernel(P3Args a) {
     }
     acc0 += (double)f0;
     acc1 += (double)f1acc;
-  }
+  })
   if (EPI >= EPI_KPM) {
     const double s0 = block_sum(acc0, red);
     const double s1 = block_sum(acc1, red);
     if (threadIdx.x == 0) {
-      double* p = a.partials + ((long long)v * gridDim.x + blockIdx.x) * 2;
+      double* p = a.partials + ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * 2;
       p[0] = s0;
       p[1] = s1;
     }

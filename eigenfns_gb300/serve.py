@@ -2,14 +2,14 @@
 
 Requests (structure seed and size, grid, Bloch k, number of bands, tolerance)
 arrive over time. The server admits a waiting request as soon as a slot is free
-and its device-memory footprint fits the budget, and runs every admitted solve
-concurrently on its own CUDA stream, so the kernels of small solves overlap on
-the device and one solve's host-side steps (fp64 eigh, convergence decisions)
-overlap with the others' device work. Solver state (blocks, locked set,
-operator tables, scratch) stays on the device for the life of the request and is
-released when it finishes. Each solve is the plain deflated block LOBPCG of
-eigenfns_gb300.solver; a solve's arithmetic does not depend on what runs beside
-it, so its result is the same alone and in the mix.
+and its device-memory footprint fits the budget, and adds its solve to the running
+batch: all admitted solves advance in lock step (eigenfns_gb300.batched), sharing one
+host transfer and one device synchronisation per step, so a request that arrives
+while others run joins at the next step and its work overlaps theirs on the device.
+Solver state (blocks, locked set, operator tables, scratch) stays on the device for
+the life of the request and is released when it finishes. Each solve is the plain
+deflated block LOBPCG of eigenfns_gb300.solver with the same kernels in the same
+order as alone, so its result is the same alone and in the mix.
 
 `run_plain` processes the same requests one at a time (the plain path) for the
 served-vs-plain comparison.
@@ -17,14 +17,12 @@ served-vs-plain comparison.
 from __future__ import annotations
 
 import math
-import threading
 import time
 from dataclasses import dataclass, field
 
 import numpy as np
 import torch
 
-from . import blas
 
 
 @dataclass
@@ -75,92 +73,92 @@ def footprint_bytes(req: SolveRequest) -> int:
     return int((cap + slabs + extra) * vec + theta_ws + tables)
 
 
-def _solve_one(req: SolveRequest, device: torch.device):
+def _operator(req: SolveRequest, device: torch.device):
     from .operator import MaxwellOperator
-    from .solver import lobpcg_blocks
     from .structure import make_structure
     eps, L, _ = make_structure(req.nodes, req.grid, seed=req.seed)
-    op = MaxwellOperator(eps, L, k_frac=req.k_frac, device=device)
+    return MaxwellOperator(eps, L, k_frac=req.k_frac, device=device)
+
+
+def _steps(req: SolveRequest, op, check_tc: bool):
+    from .solver import lobpcg_steps
     m, guard = req.block()
-    vals, vecs, st = lobpcg_blocks(op, req.nev, m=m, guard=guard, tol=req.tol, seed=req.seed,
-                                   verbose=False)
+    return lobpcg_steps(op, req.nev, m=m, guard=guard, tol=req.tol, seed=req.seed,
+                        verbose=False, check_tc=check_tc)
+
+
+def _solve_one(req: SolveRequest, device: torch.device):
+    from .solver import run_steps
+    op = _operator(req, device)
+    vals, vecs, st = run_steps(_steps(req, op, True))
     del vecs, op
     return vals, st
 
 
 class EigenServer:
-    """Admission by device-memory footprint, one CUDA stream per running solve."""
+    """Admission by device-memory footprint; admitted solves run in one lock-step batch."""
 
-    def __init__(self, budget_bytes: float = 160e9, max_concurrent: int = 8, device=None):
+    def __init__(self, budget_bytes: float = 160e9, max_concurrent: int = 16, device=None):
         self.budget = float(budget_bytes)
         self.max_concurrent = int(max_concurrent)
         self.device = torch.device(device) if device is not None else torch.device(
             "cuda", torch.cuda.current_device())
-        self._lock = threading.Lock()
         self._used = 0.0
-        self._running = 0
         self.peak_concurrent = 0
         self.peak_used = 0.0
         self.errors: list = []
-
-    def _worker(self, req: SolveRequest, fp: float, t0: float, results: list, done: threading.Event):
-        stream = torch.cuda.Stream(device=self.device)
-        try:
-            with torch.cuda.device(self.device), torch.cuda.stream(stream):
-                start = time.perf_counter() - t0
-                vals, st = _solve_one(req, self.device)
-                stream.synchronize()
-                end = time.perf_counter() - t0
-            results.append(SolveResult(req.rid, vals, max(r["max_res_locked"] for r in st.rounds),
-                                       req.arrival, start, end, st.theta_applications, st.iterations))
-        except Exception as exc:  # surfaced to the caller after the run
-            self.errors.append((req.rid, repr(exc)))
-        finally:
-            with torch.cuda.device(self.device), torch.cuda.stream(stream):
-                blas.release_workspaces(stream)
-            with self._lock:
-                self._used -= fp
-                self._running -= 1
-            done.set()
+        self.steps = 0
 
     def run(self, requests, realtime: bool = True) -> list:
         """Serve `requests` (arrival times honoured when `realtime`); returns results."""
+        from .batched import BatchedSolves
         pending = sorted(requests, key=lambda r: r.arrival)
         for r in pending:
             if footprint_bytes(r) > self.budget:
                 raise ValueError(f"request {r.rid} needs {footprint_bytes(r) / 1e9:.1f} GB, "
                                  f"above the {self.budget / 1e9:.1f} GB budget")
         results: list = []
-        threads = []
-        wake = threading.Event()
+        batch = BatchedSolves()
+        running: dict = {}            # rid -> (request, footprint, start, operator)
         t0 = time.perf_counter()
-        while pending:
-            now = time.perf_counter() - t0
-            admitted = False
-            with self._lock:
-                head = pending[0]
-                fp = footprint_bytes(head)
-                arrived = (not realtime) or head.arrival <= now
-                if arrived and self._running < self.max_concurrent and self._used + fp <= self.budget:
+
+        def finish(done: dict):
+            for rid, res in done.items():
+                req, fp, start, _ = running.pop(rid)
+                self._used -= fp
+                if isinstance(res, Exception):
+                    self.errors.append((rid, repr(res)))
+                    continue
+                vals, vecs, st = res
+                del vecs
+                results.append(SolveResult(rid, vals, max(r["max_res_locked"] for r in st.rounds),
+                                           req.arrival, start, time.perf_counter() - t0,
+                                           st.theta_applications, st.iterations))
+
+        with torch.cuda.device(self.device):
+            while pending or len(batch):
+                now = time.perf_counter() - t0
+                while pending:
+                    head = pending[0]
+                    fp = footprint_bytes(head)
+                    arrived = (not realtime) or head.arrival <= now
+                    if not (arrived and len(running) < self.max_concurrent
+                            and self._used + fp <= self.budget):
+                        break
                     pending.pop(0)
                     self._used += fp
-                    self._running += 1
-                    self.peak_concurrent = max(self.peak_concurrent, self._running)
+                    start = time.perf_counter() - t0
+                    op = _operator(head, self.device)
+                    running[head.rid] = (head, fp, start, op)
+                    self.peak_concurrent = max(self.peak_concurrent, len(running))
                     self.peak_used = max(self.peak_used, self._used)
-                    admitted = True
-            if admitted:
-                th = threading.Thread(target=self._worker, args=(head, fp, t0, results, wake),
-                                      daemon=True)
-                th.start()
-                threads.append(th)
-                continue
-            wait = 0.05
-            if realtime and head.arrival > now:
-                wait = min(wait, head.arrival - now)
-            wake.wait(timeout=max(wait, 1e-3))
-            wake.clear()
-        for th in threads:
-            th.join()
+                    finish(batch.add(head.rid, _steps(head, op, False)))
+                if len(batch):
+                    finish(batch.step())
+                elif pending and realtime:
+                    time.sleep(max(min(pending[0].arrival - (time.perf_counter() - t0), 0.05), 1e-4))
+            self.steps = batch.steps
+            torch.cuda.synchronize(self.device)
         if self.errors:
             raise RuntimeError(f"{len(self.errors)} request(s) failed: {self.errors[:3]}")
         return sorted(results, key=lambda r: r.rid)

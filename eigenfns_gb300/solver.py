@@ -92,8 +92,9 @@ def _theta(op, X, stats, out=None):
     return op.theta(X, out=out)
 
 
-def _ortho_inplace(X: torch.Tensor, passes: int = 2, drop: float = _SVQB_DROP) -> None:
-    """SVQB on a contiguous block slot, written back into the slot.
+def _ortho_steps(X: torch.Tensor, passes: int = 2, drop: float = _SVQB_DROP):
+    """SVQB on a contiguous block slot, written back into the slot (a step generator:
+    it yields the one device matrix it reads on the host).
 
     The first pass is the reference's SVQB (host fp64 eigh with the 1e-5 drop). After it
     every row is unit or zero, so the second pass is a well-conditioned re-orthonormalisation
@@ -106,12 +107,34 @@ def _ortho_inplace(X: torch.Tensor, passes: int = 2, drop: float = _SVQB_DROP) -
         if p > 0 and m <= dense.MAX_N:
             C, _ = dense.cholqr_coeffs(gram(X, X), tol=drop)
         else:
-            C, _ = svqb_coeffs(gram(X, X).cpu().numpy(), drop)
+            Gh = yield gram(X, X)
+            C, _ = svqb_coeffs(Gh, drop)
             C = C.astype(np.complex64)
         if m <= 32:
             rotate(C, X, X)
         else:
             X.copy_(rotate(C, X))
+
+
+def _ortho_inplace(X: torch.Tensor, passes: int = 2, drop: float = _SVQB_DROP) -> None:
+    run_steps(_ortho_steps(X, passes, drop))
+
+
+def _to_host(req):
+    if isinstance(req, tuple):
+        return tuple(t.cpu().numpy() for t in req)
+    return req.cpu().numpy()
+
+
+def run_steps(gen):
+    """Drive a step generator alone: each yielded device tensor (or tuple of tensors) is
+    read on the host and sent back as numpy; returns the generator's return value."""
+    try:
+        req = next(gen)
+        while True:
+            req = gen.send(_to_host(req))
+    except StopIteration as stop:
+        return stop.value
 
 
 def _normalize_rows(X: torch.Tensor, floor: float) -> None:
@@ -139,27 +162,32 @@ def _rr_gram(act: torch.Tensor, hact: torch.Tensor, m: int) -> torch.Tensor:
     return A
 
 
-def _ritz_residuals(X, HX, R, normalize: bool):
+def _ritz_steps(X, HX, R, normalize: bool):
     """(lam, relres, |x|) for the rows of X, with R = HX - lam X written into `R`.
 
     One pass for <x, Θx>, |x|^2, |Θx|^2 and one fused pass that forms R and |R|^2;
-    the small per-row vectors reach the host in a single copy."""
+    the small per-row vectors reach the host in a single copy (the one yield)."""
     st = blas.rowstats(X, HX)
     lam_d = st[:, 0] / torch.clamp(st[:, 2], min=1e-30) if normalize else st[:, 0].contiguous()
     r2 = blas.residual_norms(HX, X, lam_d, R)
-    h = torch.cat([lam_d[:, None], st[:, 2:4], r2[:, None]], dim=1).cpu().numpy()
+    h = yield torch.cat([lam_d[:, None], st[:, 2:4], r2[:, None]], dim=1)
     lam, xx, hh, rr = h[:, 0], h[:, 1], h[:, 2], h[:, 3]
     rn = np.sqrt(np.maximum(rr, 0.0)) / np.maximum(np.sqrt(np.maximum(hh, 0.0)), 1e-30)
     return lam, rn, np.sqrt(np.maximum(xx, 0.0))
 
 
-def lobpcg_blocks(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
-                  maxit: int = 400, seed: int = 0, precond_shift: str = "median",
-                  verbose: bool = True, log_every: int = 0, initial_locked=None,
-                  initial_vals=None, on_block=None, locked_storage: str = "auto",
-                  theta_chunk: int = 0, normalize_rq: bool = True, deflate_chunk: int | None = None,
-                  autotune: bool | None = None):
-    """Bottom-up deflated block LOBPCG. Returns (eigenvalues, locked_vectors, stats).
+def lobpcg_steps(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
+                 maxit: int = 400, seed: int = 0, precond_shift: str = "median",
+                 verbose: bool = True, log_every: int = 0, initial_locked=None,
+                 initial_vals=None, on_block=None, locked_storage: str = "auto",
+                 theta_chunk: int = 0, normalize_rq: bool = True, deflate_chunk: int | None = None,
+                 autotune: bool | None = None, check_tc: bool = True):
+    """Bottom-up deflated block LOBPCG as a step generator (see lobpcg_blocks).
+
+    Every point where the algorithm needs device data on the host (residuals, the SVQB
+    and P-whitening Grams, the Rayleigh-Ritz matrix) is a `yield` of the device tensor(s);
+    the driver sends back the numpy copy. run_steps drives one solve; the batched driver
+    (eigenfns_gb300.batched) advances many solves between one shared host transfer.
 
     `autotune` (default: on when EF_AUTOTUNE=1) times the operator pipeline and the
     Gram schedules of this block size once on the running GPU before the solve and
@@ -212,14 +240,14 @@ def lobpcg_blocks(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
             _normalize_rows(Xr, 1e-30)
         block_no += 1
         deflate(X, locked, deflate_chunk)
-        _ortho_inplace(X)
+        yield from _ortho_steps(X)
         _theta(op, X, stats, out=HX)
         have_p = False
         n_lock = min(m - guard, nev - locked_vals.size)
         it = 0
         for it in range(maxit):
             # R = HX - lam X lands in the W slot, where the preconditioner needs it
-            lam, rn, xnorm = _ritz_residuals(X, HX, W, False)
+            lam, rn, xnorm = yield from _ritz_steps(X, HX, W, False)
             dead_rows = xnorm < 0.5
             lam_h = np.where(dead_rows, np.inf, lam)
             rn = np.where(dead_rows, np.inf, rn)
@@ -236,12 +264,12 @@ def lobpcg_blocks(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
             deflate(W, locked, deflate_chunk)
             for _ in range(2):
                 rotate(gram(X, W).to(torch.complex64), X, W, -1)
-            _ortho_inplace(W)
+            yield from _ortho_steps(W)
             if have_p:
                 XW = S[m:3 * m]
                 for _ in range(2):
                     rotate(gram(XW, P).to(torch.complex64), XW, P, -1)
-                Tp, keepp = svqb_coeffs(gram(P, P).cpu().numpy())
+                Tp, keepp = svqb_coeffs((yield gram(P, P)))
                 if not keepp.any():
                     have_p = False
                 elif m <= 32:
@@ -257,8 +285,8 @@ def lobpcg_blocks(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
             nb = int(act.shape[0])
             A_d = _rr_gram(act, hact, m)
             rows_d = blas.rowstats(act, act)[:, 2]
-            A = A_d.cpu().numpy()
-            rownorm = np.sqrt(np.maximum(rows_d.cpu().numpy(), 0))
+            A, rows_h = yield (A_d, rows_d)
+            rownorm = np.sqrt(np.maximum(rows_h, 0))
             A = (A + A.conj().T) / 2
             dead = rownorm < 0.5
             penalty = max(_RR_DEAD_PENALTY, 100.0 * float(np.abs(np.diag(A)).max()))
@@ -279,7 +307,7 @@ def lobpcg_blocks(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
             _normalize_rows(S[0:2 * m], 1e-20)
             _theta(op, X, stats, out=HX)
         _theta(op, X, stats, out=HX)
-        lam, rn, xnorm = _ritz_residuals(X, HX, W, normalize_rq)
+        lam, rn, xnorm = yield from _ritz_steps(X, HX, W, normalize_rq)
         lam = np.where(xnorm < 0.5, np.inf, lam)
         rn = np.where(xnorm < 0.5, np.inf, rn)
         order = np.argsort(lam)
@@ -304,9 +332,10 @@ def lobpcg_blocks(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
                   f"elapsed {time.perf_counter() - t0:6.1f}s", flush=True)
         del Xl
     del slabs, HS
-    torch.cuda.synchronize(dev)
-    if blas.tc_error():
-        raise RuntimeError("a tensor-core kernel timed out waiting on its pipeline; results invalid")
+    if check_tc:
+        torch.cuda.synchronize(dev)
+        if blas.tc_error():
+            raise RuntimeError("a tensor-core kernel timed out waiting on its pipeline; results invalid")
     stats.wall_seconds = time.perf_counter() - t0
     if locked_vals.size > 1 and (np.diff(locked_vals) < -1e-6 * np.abs(locked_vals[1:])).any():
         warnings.warn("locked eigenvalues non-monotone: a band was recovered out of order; "
@@ -314,6 +343,32 @@ def lobpcg_blocks(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
     order = np.argsort(locked_vals, kind="stable")
     locked = locked_buf[:n_locked_now].index_select(0, torch.from_numpy(order).to(dev))
     return locked_vals[order][:nev], locked, stats
+
+
+def lobpcg_blocks(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
+                  maxit: int = 400, seed: int = 0, precond_shift: str = "median",
+                  verbose: bool = True, log_every: int = 0, initial_locked=None,
+                  initial_vals=None, on_block=None, locked_storage: str = "auto",
+                  theta_chunk: int = 0, normalize_rq: bool = True, deflate_chunk: int | None = None,
+                  autotune: bool | None = None):
+    """Bottom-up deflated block LOBPCG. Returns (eigenvalues, locked_vectors, stats).
+
+    `autotune` (default: on when EF_AUTOTUNE=1) times the operator pipeline and the
+    Gram schedules of this block size once on the running GPU before the solve and
+    reuses the cached choice afterwards (eigenfns_gb300.tune).
+
+    Working set: two (3m, 2, G, G, G) slabs holding the blocks as [P; X; W] (the
+    Rayleigh-Ritz basis is contiguous, so its Gram is one call and the Ritz
+    combination writes [P_new; X_new] in one pass into the other slab) and one
+    slab of operator images [ΘP; ΘX; ΘW]. The basis order [P, X, W] is a
+    permutation of the reference's [X, W, P]; the Ritz pairs are the same.
+    """
+    return run_steps(lobpcg_steps(op, nev, m=m, guard=guard, tol=tol, maxit=maxit, seed=seed,
+                                  precond_shift=precond_shift, verbose=verbose, log_every=log_every,
+                                  initial_locked=initial_locked, initial_vals=initial_vals,
+                                  on_block=on_block, locked_storage=locked_storage,
+                                  theta_chunk=theta_chunk, normalize_rq=normalize_rq,
+                                  deflate_chunk=deflate_chunk, autotune=autotune))
 
 
 def lobpcg_blocks_resumable(op, nev, checkpointer=None, resume=False, **kw):

@@ -5,7 +5,6 @@ tests/test_gpu_serve.py)."""
 from __future__ import annotations
 
 import contextlib
-import threading
 import time
 
 import numpy as np
@@ -15,22 +14,22 @@ torch = pytest.importorskip("torch")
 
 
 class _Stream:
-    def __init__(self, device=None):
-        pass
-
     def synchronize(self):
         pass
 
 
 @pytest.fixture()
 def fake_server(monkeypatch):
-    from eigenfns_gb300 import blas, serve
-    monkeypatch.setattr(torch.cuda, "Stream", _Stream)
+    """The server with its solves replaced by step generators that yield CPU tensors a
+    few times and return made-up eigenvalues (the batch driver's host transfer becomes a
+    no-op), so admission, batching and result order are exercised without a GPU."""
+    from eigenfns_gb300 import batched, blas, serve
     monkeypatch.setattr(torch.cuda, "device", lambda d: contextlib.nullcontext())
-    monkeypatch.setattr(torch.cuda, "stream", lambda s: contextlib.nullcontext())
     monkeypatch.setattr(torch.cuda, "synchronize", lambda d=None: None)
-    monkeypatch.setattr(blas, "release_workspaces", lambda stream=None: None)
-    state = {"running": 0, "peak": 0, "lock": threading.Lock()}
+    monkeypatch.setattr(torch.cuda, "current_stream", lambda d=None: _Stream())
+    monkeypatch.setattr(batched, "_request_to_host", lambda req: req)
+    monkeypatch.setattr(blas, "tc_error", lambda: 0)
+    state = {"running": 0, "peak": 0}
 
     class _Stats:
         def __init__(self, req):
@@ -38,20 +37,29 @@ def fake_server(monkeypatch):
             self.theta_applications = 10 * req.nev
             self.iterations = req.nev
 
-    def fake_solve(req, device):
-        with state["lock"]:
-            state["running"] += 1
-            state["peak"] = max(state["peak"], state["running"])
-        if req.seed < 0:
-            with state["lock"]:
-                state["running"] -= 1
-            raise RuntimeError("planted failure")
-        time.sleep(0.02)
-        vals = np.sort(np.random.default_rng(req.seed).random(req.nev)) + req.grid
-        with state["lock"]:
+    def fake_steps(req, op, check_tc):
+        state["running"] += 1
+        state["peak"] = max(state["peak"], state["running"])
+        try:
+            for _ in range(2 + req.nev % 3):
+                h = yield torch.zeros(2)
+                assert h.shape == (2,)
+                if req.seed < 0:
+                    raise RuntimeError("planted failure")
+            time.sleep(0.002)
+            vals = np.sort(np.random.default_rng(req.seed).random(req.nev)) + req.grid
+            return vals, None, _Stats(req)
+        finally:
             state["running"] -= 1
-        return vals, _Stats(req)
 
+    def fake_solve(req, device):
+        from eigenfns_gb300.solver import run_steps
+        monkeypatch.setattr("eigenfns_gb300.solver._to_host", lambda r: r.numpy())
+        vals, _, st = run_steps(fake_steps(req, None, True))
+        return vals, st
+
+    monkeypatch.setattr(serve, "_operator", lambda req, device: None)
+    monkeypatch.setattr(serve, "_steps", fake_steps)
     monkeypatch.setattr(serve, "_solve_one", fake_solve)
     return serve, state
 
