@@ -72,6 +72,46 @@ def _theta_flops_per_voxel(G: int) -> float:
     return 6 * 5 * 3 * math.log2(G) + 40
 
 
+def _fp32_roof(dev) -> dict:
+    """Measured FP32 FMA rate of this GPU (ef_fma_probe): scalar FFMA and paired FFMA2."""
+    import ctypes
+    import torch
+    from eigenfns_gb300._lib import call, load
+    blocks, iters = 152 * 8, 4096
+    out = torch.empty(blocks * 256, dtype=torch.float32, device=dev)
+    res = {}
+    for name, paired in (("ffma", 0), ("ffma2", 1)):
+        best = 0.0
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            call("ef_fma_probe", out.data_ptr(), blocks, iters, paired, torch.cuda.current_stream().cuda_stream)
+            e1.record()
+            torch.cuda.synchronize()
+            best = max(best, load().ef_fma_probe_flops(blocks, iters) / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+        res[name + "_TFLOPs"] = best
+    res["peak_TFLOPs"] = max(res.values())
+    return res
+
+
+def _accuracy(vals, eps) -> dict | None:
+    """Eigenvalue error of this solve against the complex128 run of the same method on the
+    same structure (tests/golden/fp64_n1000_g128_gamma.npz), over the bands it holds."""
+    import hashlib
+    import numpy as np
+    p = ROOT / "tests" / "golden" / "fp64_n1000_g128_gamma.npz"
+    if not p.exists():
+        return None
+    d = np.load(p)
+    if hashlib.sha256(np.ascontiguousarray(eps).tobytes()).hexdigest() != str(d["eps_sha256"]):
+        return {"note": "structure differs from the FP64 fixture"}
+    ref = d["vals"]
+    n = min(len(ref), len(vals))
+    err = np.abs(np.asarray(vals[:n]) - ref[:n]) / ref[:n]
+    return {"bands": int(n), "max_rel_err_vs_fp64": float(err.max()),
+            "median_rel_err_vs_fp64": float(np.median(err)), "fp64_tol": float(d["tol"])}
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
 
@@ -276,6 +316,48 @@ def _interior_steps(dev) -> dict:
     return out
 
 
+BATCHED_KINDS = ((64, 32, 16, 16, 4), (216, 48, 32, 32, 8), (512, 64, 48, 32, 8))  # N, grid, bands, m, guard
+
+
+def _batched_instances(dev, seeds_per_kind: int) -> dict:
+    """The 48-instance batched workload: one lock-step batch against one-at-a-time solves."""
+    import numpy as np
+    import torch
+    from eigenfns_gb300.batched import lobpcg_batched
+    from eigenfns_gb300.operator import MaxwellOperator
+    from eigenfns_gb300.solver import lobpcg_blocks
+    from eigenfns_gb300.structure import bz_kpoint, make_structure
+    inst = []
+    for nodes, grid, nev, m, guard in BATCHED_KINDS:
+        for j in range(seeds_per_kind):
+            seed = 1000 * nodes + j
+            eps, L, _ = make_structure(nodes, grid, seed=seed)
+            inst.append((MaxwellOperator(eps, L, k_frac=bz_kpoint(seed), device=dev), nev, m, guard, seed))
+    # warm both paths (kernels, plans, workspaces) on one instance of each kind
+    for k in range(len(BATCHED_KINDS)):
+        op, nev, m, g, s = inst[k * seeds_per_kind]
+        lobpcg_blocks(op, nev, m=m, guard=g, tol=1e-4, seed=s, verbose=False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    alone = [lobpcg_blocks(op, nev, m=m, guard=g, tol=1e-4, seed=s, verbose=False)
+             for op, nev, m, g, s in inst]
+    torch.cuda.synchronize()
+    t_alone = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    batch = lobpcg_batched([i[0] for i in inst], [i[1] for i in inst], m=[i[2] for i in inst],
+                           guard=[i[3] for i in inst], tol=1e-4, seeds=[i[4] for i in inst])
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    modes = sum(len(v) for v, _, _ in batch)
+    diff = max(float(np.abs(a[0] - b[0]).max() / np.abs(a[0]).max()) for a, b in zip(alone, batch))
+    return {"workload": (f"{len(inst)} instances: N in (64, 216, 512) x {seeds_per_kind} seeds on "
+                         "32^3/48^3/64^3, k uniform in the first BZ, 16/32/48 bands, tol 1e-4"),
+            "batched_s": t_batch, "one_at_a_time_s": t_alone,
+            "batched_modes_per_s": modes / t_batch, "one_at_a_time_modes_per_s": modes / t_alone,
+            "speedup": t_alone / t_batch, "max_rel_diff_batched_vs_alone": diff,
+            "theta_applications": int(sum(st.theta_applications for _, _, st in batch))}
+
+
 def run_ours(args, w):
     import numpy as np
     import torch
@@ -351,9 +433,11 @@ def run_ours(args, w):
         gbs = tq["bytes"] / (tq["total_ms"] * 1e-3) / 1e9
         vecs_per_s = tq["bytes"] / (32.0 * G ** 3 + 4.0 * G ** 3 / max(w["block"], 1)) / (tq["total_ms"] * 1e-3)
         tflops = vecs_per_s * _theta_flops_per_voxel(G) * G ** 3 / 1e12
-        fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12       # FMA lanes x 2 flops x max SM clock
+        fp32 = _fp32_roof(dev)
+        fp32_peak = fp32["peak_TFLOPs"]
         theta_roof = {"achieved_GBs": gbs, "hbm_frac": gbs / peak, "achieved_TFLOPs": tflops,
-                      "fp32_peak_TFLOPs": fp32_peak, "fp32_frac": tflops / fp32_peak,
+                      "fp32_peak_TFLOPs": fp32_peak, "fp32_peak_source": "measured (ef_fma_probe)",
+                      "fp32_probe": fp32, "fp32_frac": tflops / fp32_peak,
                       "us_per_vector": 1e6 / vecs_per_s,
                       "traffic_per_vector": TRAFFIC_RATIO["theta"] * 32.0 * G ** 3}
 
@@ -387,15 +471,15 @@ def run_ours(args, w):
 
     # served vs plain: a seeded Poisson stream of smaller eigensolve requests (N in
     # {64, 216, 512} on 32^3/48^3/64^3, random Bloch k, 8-48 bands) solved by the
-    # continuously batched server (device-memory admission, one stream per solve)
-    # and by the plain one-at-a-time path
+    # continuously batched server (device-memory admission, lock-step batch) and by
+    # the plain one-at-a-time path
     served = None
     if not args.no_served:
         from eigenfns_gb300.serve import EigenServer, poisson_requests, run_plain, summarize
         reqs = poisson_requests(args.served_requests, seed=2025 + rank, rate_hz=40.0)
         run_plain(reqs[:2])                       # warm the small-grid kernels
         t0 = time.perf_counter()
-        srv = EigenServer(budget_bytes=160e9, max_concurrent=8, device=dev)
+        srv = EigenServer(budget_bytes=160e9, max_concurrent=32, device=dev)
         res_s = srv.run(reqs, realtime=True)
         wall_s = time.perf_counter() - t0
         t0 = time.perf_counter()
@@ -404,9 +488,16 @@ def run_ours(args, w):
         ss, sp = summarize(res_s, wall_s), summarize(res_p, wall_p)
         same = max(float(np.abs(a.vals - b.vals).max() / np.abs(b.vals).max()) for a, b in zip(res_s, res_p))
         served = {"workload": f"{len(reqs)} Poisson requests (40/s): N in (64, 216, 512) on 32^3/48^3/64^3, "
-                              "random k, 8-48 bands, tol 1e-4; 160 GB admission budget, 8 slots",
+                              "random k, 8-48 bands, tol 1e-4; 160 GB admission budget, 32 slots",
                   "served": ss, "plain": sp, "speedup": ss["modes_per_s"] / sp["modes_per_s"],
                   "peak_concurrent": srv.peak_concurrent, "max_rel_diff_served_vs_plain": same}
+
+    # batched launch of 48 uneven instances: rod networks with N in {64, 216, 512} (16 seeds
+    # each) on 32^3/48^3/64^3, a k-point drawn in each supercell's first Brillouin zone,
+    # 16/32/48 lowest bands; all solved in one lock-step batch against one at a time
+    batched = None
+    if not args.no_batched:
+        batched = _batched_instances(dev, args.batched_seeds)
 
     # interior-window kernels at their configuration sizes (N = 10,000 structure):
     # fused KPM steps at 256^3 on 16 complex Rademacher probes and fused bandpass
@@ -445,9 +536,11 @@ def run_ours(args, w):
         "kernels": {k: {"share_of_step": v["total_ms"] / sum(step_ms), "calls": v["calls"],
                         "mean_ms": v["mean_ms_per_call"], "GB/s": v["gbs"], "TFLOP/s": v["tflops"]}
                     for k, v in ops.items()},
-        "cpu_baseline": cpu, "e2e": e2e, "served": served, "interior": interior, "clocks": clocks,
+        "cpu_baseline": cpu, "e2e": e2e, "served": served, "batched": batched, "interior": interior,
+        "clocks": clocks,
         "gpu_launches": launches,
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+        "accuracy": _accuracy(vals_list[-1], eps),
         "solve": {"theta_applications": st0.theta_applications, "iterations": st0.iterations,
                   "blocks": len(st0.rounds),
                   "max_res_locked": max(r["max_res_locked"] for r in st0.rounds),
@@ -467,7 +560,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-interior", action="store_true")
-    ap.add_argument("--served-requests", type=int, default=24)
+    ap.add_argument("--served-requests", type=int, default=48)
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batched-seeds", type=int, default=16,
+                    help="seeds per node count in the batched-instances workload (16 = 48 instances)")
     ap.add_argument("--grid", type=int, default=None, help="override the grid (smaller probes)")
     ap.add_argument("--bands", type=int, default=None)
     ap.add_argument("--tol", type=float, default=None)

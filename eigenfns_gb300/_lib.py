@@ -62,6 +62,8 @@ SIGNATURES = {
     "ef_energy_density": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _sz, _vp]),
     "ef_gram_tc": (_i, [_vp, _vp, _i, _i, _ll, _vp, _vp, _vp, _sz, _vp]),
     "ef_rotate": (_i, [_vp, _vp, _vp, _i, _i, _ll, _i, _vp]),
+    "ef_fma_probe_flops": (C.c_longlong, [_i, _i]),
+    "ef_fma_probe": (_i, [_vp, _i, _i, _i, _vp]),
     "ef_cholqr_f64": (_i, [_vp, _i, _i, _vp, _vp, _d, _vp]),
     "ef_eigh_f64_workspace_bytes": (_sz, [_i, _i]),
     "ef_eigh_f64": (_i, [_vp, _i, _i, _vp, _vp, _vp, _sz, _vp, _vp]),

@@ -180,6 +180,12 @@ int ef_gram_tc(const float* A, const float* B, int ma, int mb, long long K, doub
  * variable EF_ROTATE_KERNEL=simt selects the fp32 CUDA-core kernel instead. */
 int ef_rotate(const float* C, const float* S, float* out, int m_in, int m_out, long long K,
               int mode, void* stream);
+/* ---- arithmetic-rate probe (no counterpart in the reference: measures the FP32 roof
+ * the operator's FFT work is compared against) ----
+ * `blocks` CTAs of 256 threads, each thread 8 independent fp32 FMA chains of `iters`
+ * steps (paired = 1: four FFMA2 pairs); out holds blocks*256 floats. */
+long long ef_fma_probe_flops(int blocks, int iters);
+int ef_fma_probe(float* out, int blocks, int iters, int paired, void* stream);
 /* ---- small dense fp64 problems on the device (solver.py:46-66, 113-126, 281-301) ----
  * Batched, one CTA per problem; matrices complex128 (n, n) row-major, 1 <= n <= 96,
  * consecutive in memory for the batch. */
