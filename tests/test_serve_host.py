@@ -42,6 +42,7 @@ def fake_server(monkeypatch):
         state["peak"] = max(state["peak"], state["running"])
         try:
             for _ in range(2 + req.nev % 3):
+                time.sleep(0.003)                   # device work of one step
                 h = yield torch.zeros(2)
                 assert h.shape == (2,)
                 if req.seed < 0:
