@@ -3,13 +3,14 @@
 Each solve is the deflated block LOBPCG of eigenfns_gb300.solver written as a step
 generator (solver.lobpcg_steps): the algorithm runs until it needs device data on the
 host (residual norms, an SVQB Gram, the Rayleigh-Ritz matrix) and yields those device
-tensors. The driver here advances every active solve to its next such point, which
-queues that solve's kernels on the shared stream, then copies all the requested
-tensors to pinned host memory and synchronizes once for the whole batch, and resumes
-each solve with its data. Per step the host therefore waits once for all instances
-instead of once per instance, the GPU runs the instances' kernels back to back, and
-each solve's small host work (fp64 eigh) overlaps the device work queued by the solves
-after it. Solves may join and leave between steps (continuous batching, see
+tensors, or a request for the fp64 eigendecomposition of one. The driver here advances
+every active solve to its next such point, which queues that solve's kernels on the
+shared stream, then copies all the requested tensors to pinned host memory and
+synchronizes once for the whole batch, runs the step's eigendecompositions side by
+side on host threads, and resumes each solve with its data. Per step the host
+therefore waits once for all instances instead of once per instance, the GPU runs the
+instances' kernels back to back, and the instances' fp64 eigh calls share the host
+cores. Solves may join and leave between steps (continuous batching, see
 eigenfns_gb300.serve). A solve's kernels and their order are exactly those of the solve
 run alone, so its results are identical alone and in the batch.
 
@@ -19,10 +20,31 @@ scripts/exp/chain_i6resume.sh).
 """
 from __future__ import annotations
 
+import os
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
 import torch
 
 from . import blas
-from .solver import lobpcg_steps
+from .solver import HostEigh, lobpcg_steps
+
+_POOL = None
+
+
+def _pool() -> ThreadPoolExecutor:
+    """Host threads for the solves' fp64 eigh calls (LAPACK releases the GIL)."""
+    global _POOL
+    if _POOL is None:
+        _POOL = ThreadPoolExecutor(max_workers=max(1, min(32, os.cpu_count() or 1)))
+    return _POOL
+
+
+class _EighOnHost:
+    __slots__ = ("A",)
+
+    def __init__(self, A):
+        self.A = A
 
 
 def _pinned_copy(t: torch.Tensor) -> torch.Tensor:
@@ -32,6 +54,8 @@ def _pinned_copy(t: torch.Tensor) -> torch.Tensor:
 
 
 def _request_to_host(req):
+    if isinstance(req, HostEigh):
+        return _EighOnHost(_pinned_copy(req.A))
     if isinstance(req, tuple):
         return tuple(_pinned_copy(t) for t in req)
     return _pinned_copy(req)
@@ -73,6 +97,9 @@ class BatchedSolves:
         hosts = {k: _request_to_host(req) for k, (_, req) in self._active.items()}
         torch.cuda.current_stream().synchronize()
         self.steps += 1
+        # the step's eigenproblems run side by side on the host threads
+        eigh = {k: _pool().submit(np.linalg.eigh, h.A.numpy()) for k, h in hosts.items()
+                if isinstance(h, _EighOnHost)}
         if blas.tc_error():
             # a tensor-core pipeline wait ran out in some solve since the last step: every
             # solve in flight may hold invalid data, so all of them fail
@@ -86,7 +113,8 @@ class BatchedSolves:
         for k in list(self._active):
             gen, _ = self._active[k]
             try:
-                self._active[k] = (gen, gen.send(_numpy(hosts[k])))
+                data = eigh[k].result() if k in eigh else _numpy(hosts[k])
+                self._active[k] = (gen, gen.send(data))
             except StopIteration as stop:
                 finished[k] = stop.value
                 del self._active[k]

@@ -67,21 +67,23 @@ const Plan3* find_plan3(const ef_op* op) {
 }
 
 // Plane-pass multiplier in the slot order the plane pass sees between its inverse
-// and forward transforms: slot (row R2*k1 + j, column q) of plane z holds real-space
-// x = k1 + R1*j and y = q/R2 + R1*(q%R2); stored [z][k1][q][j] so that one item's
-// R2 factors are contiguous.
-void permute_plane_table(const std::vector<float>& w, int G, int R1, int R2, std::vector<float>& out) {
+// and forward transforms: in sub-plane (z, s), slot (row XR2*k1 + j, column q) holds
+// real-space x = Q*(k1 + XR1*j) + s and y = q/YR2 + YR1*(q%YR2); stored
+// [z][s][k1][q][j] so that one item's XR2 factors are contiguous.
+void permute_plane_table(const std::vector<float>& w, const Plan3& p, std::vector<float>& out) {
+  const int G = p.G, Q = p.Q, XR1 = p.x_R1, XR2 = p.x_R2, YR1 = p.y_R1, YR2 = p.y_R2;
   out.resize(w.size());
   size_t o = 0;
   for (int z = 0; z < G; ++z)
-    for (int k1 = 0; k1 < R1; ++k1)
-      for (int q = 0; q < G; ++q) {
-        const int yr = q / R2 + R1 * (q % R2);
-        for (int j = 0; j < R2; ++j) {
-          const int xr = k1 + R1 * j;
-          out[o++] = w[((size_t)xr * G + yr) * G + z];
+    for (int s = 0; s < Q; ++s)
+      for (int k1 = 0; k1 < XR1; ++k1)
+        for (int q = 0; q < G; ++q) {
+          const int yr = q / YR2 + YR1 * (q % YR2);
+          for (int j = 0; j < XR2; ++j) {
+            const int xr = Q * (k1 + XR1 * j) + s;
+            out[o++] = w[((size_t)xr * G + yr) * G + z];
+          }
         }
-      }
 }
 
 // ---- host-side fp64 frame tables (operator.py:46-59) -----------------------------
@@ -257,7 +259,7 @@ int run_pipe(const ef_op* op, const Pipe& pp, const float2* X, float2* out, floa
       a.c0 = c0;
       a.c1 = c1;
       q->zin[pp.build == BUILD_PRECOND ? 1 : 0](dim3(sz.tiles, nb), q->smem_z, st, a);
-      q->plane(dim3(3 * G * nb / q->PL), q->smem_plane, st, a);
+      q->plane(dim3(3 * G * q->Q * nb / q->PL), q->smem_plane, st, a);
       q->zout[pp.epi](dim3(sz.tiles, nb), q->smem_z, st, a);
     } else {
       PassArgs a;
@@ -411,8 +413,8 @@ int ef_op_create(int grid, double box_size, double kx, double ky, double kz, con
   const Plan3* p3 = plan3_of_grid(G);
   std::vector<float> pinv, peps;
   if (p3) {
-    permute_plane_table(inv, G, p3->pl_R1, p3->pl_R2, pinv);
-    permute_plane_table(epsn, G, p3->pl_R1, p3->pl_R2, peps);
+    permute_plane_table(inv, *p3, pinv);
+    permute_plane_table(epsn, *p3, peps);
   }
   std::vector<float2> tw(G);
   for (int j = 0; j < G; ++j) {

@@ -48,10 +48,29 @@ def svqb_coeffs(Gm: np.ndarray, drop: float = _SVQB_DROP):
     """SVQB rotation V diag(w^-1/2) from a Gram matrix, zero columns where dropped."""
     Gm = np.asarray(Gm).astype(np.complex128)
     Gm = (Gm + Gm.conj().T) / 2
-    w, V = np.linalg.eigh(Gm)
+    return svqb_from_eig(*np.linalg.eigh(Gm), drop)
+
+
+def svqb_from_eig(w: np.ndarray, V: np.ndarray, drop: float = _SVQB_DROP):
+    """The SVQB rotation from the eigendecomposition of the (symmetrised) Gram matrix."""
     keep = w > drop * max(w.max(), 1e-300)
     scale = np.where(keep, 1.0 / np.sqrt(np.where(keep, w, 1.0)), 0.0)
     return V * scale[None, :], keep
+
+
+class HostEigh:
+    """A step generator's request for numpy.linalg.eigh of a Hermitian device matrix.
+
+    The driver returns (w, V). Single solves (run_steps) run it in place; the batched
+    driver runs the requests of all solves in a step in parallel host threads."""
+    __slots__ = ("A",)
+
+    def __init__(self, A: torch.Tensor):
+        self.A = A
+
+
+def _hermitian(G: torch.Tensor) -> torch.Tensor:
+    return 0.5 * (G + G.conj().T)
 
 
 def ortho_block(X: torch.Tensor, passes: int = 2, drop: float = _SVQB_DROP) -> torch.Tensor:
@@ -107,8 +126,8 @@ def _ortho_steps(X: torch.Tensor, passes: int = 2, drop: float = _SVQB_DROP):
         if p > 0 and m <= dense.MAX_N:
             C, _ = dense.cholqr_coeffs(gram(X, X), tol=drop)
         else:
-            Gh = yield gram(X, X)
-            C, _ = svqb_coeffs(Gh, drop)
+            w, V = yield HostEigh(_hermitian(gram(X, X)))
+            C, _ = svqb_from_eig(w, V, drop)
             C = C.astype(np.complex64)
         if m <= 32:
             rotate(C, X, X)
@@ -121,6 +140,8 @@ def _ortho_inplace(X: torch.Tensor, passes: int = 2, drop: float = _SVQB_DROP) -
 
 
 def _to_host(req):
+    if isinstance(req, HostEigh):
+        return np.linalg.eigh(req.A.cpu().numpy())
     if isinstance(req, tuple):
         return tuple(t.cpu().numpy() for t in req)
     return req.cpu().numpy()
@@ -269,7 +290,7 @@ def lobpcg_steps(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
                 XW = S[m:3 * m]
                 for _ in range(2):
                     rotate(gram(XW, P).to(torch.complex64), XW, P, -1)
-                Tp, keepp = svqb_coeffs((yield gram(P, P)))
+                Tp, keepp = svqb_from_eig(*(yield HostEigh(_hermitian(gram(P, P)))))
                 if not keepp.any():
                     have_p = False
                 elif m <= 32:
@@ -285,13 +306,13 @@ def lobpcg_steps(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
             nb = int(act.shape[0])
             A_d = _rr_gram(act, hact, m)
             rows_d = blas.rowstats(act, act)[:, 2]
-            A, rows_h = yield (A_d, rows_d)
-            rownorm = np.sqrt(np.maximum(rows_h, 0))
-            A = (A + A.conj().T) / 2
-            dead = rownorm < 0.5
-            penalty = max(_RR_DEAD_PENALTY, 100.0 * float(np.abs(np.diag(A)).max()))
-            A[np.diag_indices_from(A)] += np.where(dead, penalty, 0.0)
-            wA, VA = np.linalg.eigh(A)
+            # symmetrise and lift dead rows (|x| < 0.5) by the reference's penalty
+            # (solver.py:281-301) on the device, then the fp64 eigh on the host
+            A_s = _hermitian(A_d)
+            dead = torch.sqrt(torch.clamp(rows_d, min=0.0)) < 0.5
+            penalty = torch.clamp(100.0 * A_s.diagonal().abs().max(), min=_RR_DEAD_PENALTY)
+            A_s.diagonal().add_(torch.where(dead, penalty, torch.zeros_like(penalty)).to(A_s.dtype))
+            wA, VA = yield HostEigh(A_s)
             Cm = VA[:, :m]
             Cp = Cm.copy()
             x_rows = slice(m - off, 2 * m - off)   # rows of the X block inside the active basis
