@@ -386,6 +386,10 @@ def run_ours(args, w):
             dist.barrier()
         torch.cuda.synchronize()
 
+    # the autotuner picks the operator pipeline and the Gram schedules of this block size
+    # on this GPU (timed once, cached on disk for later runs)
+    from eigenfns_gb300 import tune
+    tuned = tune.autotune(op, w["block"])
     for _ in range(args.warmup):
         solve()
     barrier()
@@ -541,6 +545,9 @@ def run_ours(args, w):
         "gpu_launches": launches,
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
         "accuracy": _accuracy(vals_list[-1], eps),
+        "autotune": {"operator": {k: tuned["operator"][k] for k in ("passes", "subbatch_bytes", "ms")},
+                     "gram": {k: {"kernel": v["kernel"], "units": v["units"]}
+                              for k, v in tuned["gram"].items()}},
         "solve": {"theta_applications": st0.theta_applications, "iterations": st0.iterations,
                   "blocks": len(st0.rounds),
                   "max_res_locked": max(r["max_res_locked"] for r in st0.rounds),

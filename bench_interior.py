@@ -39,11 +39,15 @@ SEED = 7          # structure seed of the interior workload
 WINDOW_RATIO = 1.930 / 1.757
 
 
-def _operator(grid: int):
+def _operator(grid: int, m: int):
+    """The structure's operator, with its pipeline picked by the autotuner for blocks of m."""
+    from eigenfns_gb300 import tune
     from eigenfns_gb300.operator import MaxwellOperator
     from eigenfns_gb300.structure import make_structure
     eps, L, net = make_structure(10000, grid, seed=SEED)
-    return MaxwellOperator(eps, L), net
+    op = MaxwellOperator(eps, L)
+    choice = tune.tune_operator(op, m)
+    return op, {k: choice[k] for k in ("passes", "subbatch_bytes", "ms")}
 
 
 def run_kpm(a) -> dict:
@@ -51,7 +55,7 @@ def run_kpm(a) -> dict:
     from eigenfns_gb300 import kpm
     from eigenfns_gb300.chebyshev import lanczos_lambda_max
     t0 = time.perf_counter()
-    op, net = _operator(a.grid)
+    op, tuned = _operator(a.grid, a.probes)
     lam_max = 1.05 * lanczos_lambda_max(op)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
@@ -65,7 +69,7 @@ def run_kpm(a) -> dict:
                             probes=a.probes, seed=a.seed)
     G = a.grid
     return {"workload": f"KPM DOS N=10000 {G}^3 degree {a.degree} x {a.probes} complex probes",
-            "lam_max": lam_max, "setup_s": t1 - t0, "moments_s": t2 - t1,
+            "lam_max": lam_max, "setup_s": t1 - t0, "moments_s": t2 - t1, "pipeline": tuned,
             "theta_applications": n_theta, "theta_per_s": n_theta / (t2 - t1),
             "algorithmic_GBs": 48.0 * G ** 3 * n_theta / (t2 - t1) / 1e9,
             "counting": {"lam": lams.tolist(), "N": mean.tolist(), "se": se.tolist()}}
@@ -88,7 +92,7 @@ def run_chebsi(a) -> dict:
     from eigenfns_gb300.chebyshev import lanczos_lambda_max
     from eigenfns_gb300.run_interior import two_stage
     t0 = time.perf_counter()
-    op, net = _operator(a.grid)
+    op, tuned = _operator(a.grid, a.chunk)
     lam_max = 1.05 * lanczos_lambda_max(op)
     lam_lo, lam_hi, est_inside, est_below = choose_window(op, lam_max)
     torch.cuda.synchronize()
@@ -101,7 +105,7 @@ def run_chebsi(a) -> dict:
     G = a.grid
     return {"workload": (f"two-stage ChebSI N=10000 {G}^3 m={a.m} build {a.build_degree}x"
                          f"{a.build_outers} polish {a.polish_degree}x{a.polish_outers}"),
-            "window": [lam_lo, lam_hi], "kpm_estimate_inside": est_inside,
+            "window": [lam_lo, lam_hi], "kpm_estimate_inside": est_inside, "pipeline": tuned,
             "kpm_estimate_below": est_below, "lam_max": lam_max, "setup_s": t1 - t0,
             "solve_s": t2 - t1, "theta_applications": r["theta_applications"],
             "theta_per_s": r["theta_applications"] / (t2 - t1),
