@@ -50,3 +50,23 @@ def test_admission_respects_the_budget():
     assert len(srv.run(pair, realtime=False)) == 2 and srv.peak_concurrent == 1
     with pytest.raises(ValueError):
         EigenServer(budget_bytes=max(fps) / 4).run(reqs, realtime=False)
+
+
+def test_footprint_covers_measured_device_memory():
+    """The admission footprint of a request is at least the device memory its solve
+    allocates through torch (the peak above the level before the request), which holds
+    the blocks, the locked set, the slabs and the scratch; the operator's own tables,
+    allocated by the library, are the footprint's 20 B per voxel on top."""
+    from eigenfns_gb300 import blas
+    from eigenfns_gb300.serve import SolveRequest, _solve_one, footprint_bytes
+    for req in (SolveRequest(0, 64, 32, 21, 16, (0.1, 0.2, 0.3)),
+                SolveRequest(1, 216, 48, 22, 24, (0.0, 0.0, 0.0))):
+        blas.release_workspaces()
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        base = torch.cuda.memory_allocated()
+        torch.cuda.reset_peak_memory_stats()
+        _solve_one(req, torch.device("cuda", 0))
+        torch.cuda.synchronize()
+        used = torch.cuda.max_memory_allocated() - base
+        assert used <= footprint_bytes(req), (used, footprint_bytes(req))
