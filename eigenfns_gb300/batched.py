@@ -20,6 +20,7 @@ scripts/exp/chain_i6resume.sh).
 """
 from __future__ import annotations
 
+import contextlib
 import os
 from concurrent.futures import ThreadPoolExecutor
 
@@ -68,10 +69,18 @@ def _numpy(h):
 
 
 class BatchedSolves:
-    """Lock-step driver of step generators that share one CUDA stream."""
+    """Lock-step driver of step generators.
 
-    def __init__(self):
+    Each solve is bound to one of `streams` CUDA streams (round robin as solves join), so
+    the small kernels of different solves can run side by side on the device while each
+    solve's own kernels keep their order (its scratch buffers are per stream); a step
+    ends with one device synchronisation."""
+
+    def __init__(self, streams: int = 8):
         self._active: dict = {}     # key -> (generator, pending request)
+        self._stream_of: dict = {}
+        self._streams = [torch.cuda.Stream() for _ in range(max(1, streams))] if streams > 1 else None
+        self._next = 0
         self.steps = 0
 
     def __len__(self) -> int:
@@ -80,12 +89,24 @@ class BatchedSolves:
     def keys(self):
         return list(self._active)
 
+    def _ctx(self, key):
+        if self._streams is None:
+            return contextlib.nullcontext()
+        return torch.cuda.stream(self._stream_of[key])
+
     def add(self, key, gen) -> dict:
         """Start a solve (runs it up to its first host read). Returns {key: result} if it
         finished without reading anything (never for LOBPCG)."""
+        if self._streams is not None:
+            self._stream_of[key] = self._streams[self._next % len(self._streams)]
+            self._next += 1
+            # the solve's inputs were made on the caller's stream
+            self._stream_of[key].wait_stream(torch.cuda.current_stream())
         try:
-            self._active[key] = (gen, next(gen))
+            with self._ctx(key):
+                self._active[key] = (gen, next(gen))
         except StopIteration as stop:
+            self._stream_of.pop(key, None)
             return {key: stop.value}
         return {}
 
@@ -94,8 +115,14 @@ class BatchedSolves:
         solves that finished in this step as {key: result or the exception raised}."""
         if not self._active:
             return {}
-        hosts = {k: _request_to_host(req) for k, (_, req) in self._active.items()}
-        torch.cuda.current_stream().synchronize()
+        hosts = {}
+        for k, (_, req) in self._active.items():
+            with self._ctx(k):
+                hosts[k] = _request_to_host(req)
+        if self._streams is None:
+            torch.cuda.current_stream().synchronize()
+        else:
+            torch.cuda.synchronize()
         self.steps += 1
         # the step's eigenproblems run side by side on the host threads
         eigh = {k: _pool().submit(np.linalg.eigh, h.A.numpy()) for k, h in hosts.items()
@@ -108,19 +135,25 @@ class BatchedSolves:
             for g, _ in self._active.values():
                 g.close()
             self._active.clear()
+            self._stream_of.clear()
             return done
         finished = {}
         for k in list(self._active):
             gen, _ = self._active[k]
             try:
                 data = eigh[k].result() if k in eigh else _numpy(hosts[k])
-                self._active[k] = (gen, gen.send(data))
+                with self._ctx(k):
+                    self._active[k] = (gen, gen.send(data))
             except StopIteration as stop:
                 finished[k] = stop.value
                 del self._active[k]
             except Exception as exc:            # surfaced to the caller per solve
                 finished[k] = exc
                 del self._active[k]
+        for k in finished:
+            s = self._stream_of.pop(k, None)
+            if s is not None:                   # results are used on the caller's stream
+                torch.cuda.current_stream().wait_stream(s)
         return finished
 
     def run(self) -> dict:
@@ -132,19 +165,20 @@ class BatchedSolves:
 
 
 def lobpcg_batched(ops, nevs, m: int = 32, guard: int = 8, tol: float = 1e-4, maxit: int = 400,
-                   seeds=None, **kw) -> list:
+                   seeds=None, streams: int = 8, **kw) -> list:
     """Solve several operators' lowest eigenpairs in lock step.
 
     `ops` are MaxwellOperators (any mix of grids and k-points), `nevs` the bands wanted
     from each (an int applies to all); `m`/`guard` may also be per-instance lists.
     Returns [(eigenvalues, locked vectors, SolveStats)] in the order of `ops`, each equal
     to lobpcg_blocks(op, nev, ...) run alone; raises the first failure after the batch.
+    `streams` CUDA streams are shared round robin by the solves (1: the current stream).
     """
     n = len(ops)
     per = lambda v: list(v) if isinstance(v, (list, tuple)) else [v] * n
     nevs, ms, guards = per(nevs), per(m), per(guard)
     seeds = per(0 if seeds is None else seeds)
-    drv = BatchedSolves()
+    drv = BatchedSolves(streams)
     out = {}
     for i, op in enumerate(ops):
         out.update(drv.add(i, lobpcg_steps(op, nevs[i], m=ms[i], guard=guards[i], tol=tol,

@@ -40,7 +40,7 @@ def _solve(name, n, log, fail_at=None):
 
 def test_lock_step_shares_one_sync_per_step(driver):
     batched, log, _ = driver
-    d = batched.BatchedSolves()
+    d = batched.BatchedSolves(streams=1)
     for name, n in (("a", 3), ("b", 1), ("c", 2)):
         d.add(name, _solve(name, n, log))
     out = d.run()
@@ -52,12 +52,12 @@ def test_lock_step_shares_one_sync_per_step(driver):
 
 def test_failures_are_per_solve_and_timeouts_fail_all(driver):
     batched, log, flag = driver
-    d = batched.BatchedSolves()
+    d = batched.BatchedSolves(streams=1)
     d.add("ok", _solve("ok", 2, log))
     d.add("bad", _solve("bad", 3, log, fail_at=0))
     out = d.run()
     assert out["ok"] == ("ok", 1) and isinstance(out["bad"], ValueError)
-    d = batched.BatchedSolves()
+    d = batched.BatchedSolves(streams=1)
     d.add("x", _solve("x", 3, log))
     d.add("y", _solve("y", 3, log))
     flag["tc"] = 1
