@@ -63,8 +63,8 @@ def _peaks():
 # DRAM traffic over algorithmic bytes from single-kernel ncu captures (profiles/):
 # tc_gram_32x32_K512k.md (268.5 MB read + 5.6 MB written for 268.4 MB algorithmic),
 # tc_rotate_96x64_K512k.md (0.403 + 0.223 GB for 0.671 GB), theta_passes_128.md
-# (340 MB per vector for 71 MB algorithmic)
-TRAFFIC_RATIO = {"gram": 1.02, "rotate": 0.93, "theta": 4.8}
+# (three passes, steady state: 129.7 MB per vector for 67.1 MB algorithmic)
+TRAFFIC_RATIO = {"gram": 1.02, "rotate": 0.93, "theta": 1.93}
 # FP32 flops of one Θ application per voxel and vector: 6 complex 3-D FFTs
 # (5 N log2 N each) plus the curl, frame and multiply work (~40 per voxel)
 def _theta_flops_per_voxel(G: int) -> float:

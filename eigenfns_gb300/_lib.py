@@ -56,6 +56,7 @@ SIGNATURES = {
     "ef_gram_noalloc": (_i, [_vp, _vp, _i, _i, _ll, _vp, _vp]),
     "ef_gram_tc_workspace_bytes": (_sz, [_i, _i, _ll]),
     "ef_tc_error": (_i, [_vp]),
+    "ef_tc_error_async": (_i, [_vp, _vp]),
     "ef_tune_gram": (_i, [_i, _i, _i, _i]),
     "ef_tune_reset": (_i, []),
     "ef_energy_workspace_bytes": (_i, [_vp, _i]),

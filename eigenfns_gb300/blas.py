@@ -21,8 +21,18 @@ from ._lib import call
 _WS: dict = {}
 
 
-def _stream():
-    return torch.cuda.current_stream().cuda_stream
+try:                                    # the raw handle without torch.cuda's Python layers
+    _raw_stream = torch._C._cuda_getCurrentRawStream
+    _cur_device = torch._C._cuda_getDevice
+except AttributeError:                  # CPU-only torch build
+    _raw_stream = _cur_device = None
+
+
+def _stream(device_index: int | None = None):
+    """Handle of the current CUDA stream (of the current device, or of `device_index`)."""
+    if _raw_stream is None:
+        return torch.cuda.current_stream().cuda_stream
+    return _raw_stream(_cur_device() if device_index is None else device_index)
 
 
 def workspace(nbytes: int, device, slot: str = "blas") -> torch.Tensor:
@@ -31,7 +41,8 @@ def workspace(nbytes: int, device, slot: str = "blas") -> torch.Tensor:
     Keyed by the current CUDA stream so solves running concurrently on different
     streams (the request server) never share scratch; work on one stream is
     ordered, so reuse within a stream is safe."""
-    key = (str(device), slot, torch.cuda.current_stream(device).cuda_stream)
+    device = torch.device(device) if not isinstance(device, torch.device) else device
+    key = (str(device), slot, _stream(device.index))
     buf = _WS.get(key)
     if buf is None or buf.numel() < nbytes:
         buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
@@ -164,6 +175,12 @@ def tc_error() -> int:
     flag = ctypes.c_int(0)
     call("ef_tc_error", ctypes.addressof(flag))
     return int(flag.value)
+
+
+def tc_error_async(host_flag: torch.Tensor) -> None:
+    """Queue a copy of the tensor-core error flag into `host_flag` (a pinned int32 host
+    tensor of one element) on the current stream; the flag is not cleared."""
+    call("ef_tc_error_async", host_flag.data_ptr(), _stream())
 
 
 def raise_on_tc_error(what: str) -> None:

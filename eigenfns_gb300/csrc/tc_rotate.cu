@@ -383,7 +383,20 @@ int tc_error_flag(int* flag) {
   return EF_OK;
 }
 
+// queues a copy of the flag into host memory on a stream (the flag is not cleared)
+int tc_error_flag_async(int* host_flag, cudaStream_t st) {
+  cudaError_t e = cudaMemcpyFromSymbolAsync(host_flag, g_tc_error, sizeof(int), 0,
+                                            cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return ef_fail(EF_ERR_CUDA, cudaGetErrorString(e));
+  return EF_OK;
+}
+
 }  // namespace ef
+
+extern "C" int ef_tc_error_async(int* host_flag, void* stream) {
+  if (!host_flag) return ef_fail(EF_ERR_INVALID, "null flag");
+  return ef::tc_error_flag_async(host_flag, (cudaStream_t)stream);
+}
 
 extern "C" int ef_tc_error(int* flag) {
   if (!flag) return ef_fail(EF_ERR_INVALID, "null flag");

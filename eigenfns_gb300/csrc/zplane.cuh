@@ -567,7 +567,7 @@ Plan3 make_plan3() {
   p.zout[4] = launch_zout<OR1, OR2, Q, EPI_KPM>;
   p.zout[5] = launch_zout<OR1, OR2, Q, EPI_KPM_FIRST>;
   p.zout[6] = launch_zout<OR1, OR2, Q, EPI_KPM_COUNT>;
-  p.zout[7] = launch_zout<OR1, OR2, Q, EPI_KPM_FIRST>;
+  p.zout[7] = launch_zout<OR1, OR2, Q, EPI_KPM_FIRST>;   // first count step: same epilogue
   return p;
 }
 

@@ -3,9 +3,9 @@
 Requests (structure seed and size, grid, Bloch k, number of bands, tolerance)
 arrive over time. The server admits a waiting request as soon as a slot is free
 and its device-memory footprint fits the budget, and adds its solve to the running
-batch: all admitted solves advance in lock step (eigenfns_gb300.batched), sharing one
-host transfer and one device synchronisation per step, so a request that arrives
-while others run joins at the next step and its work overlaps theirs on the device.
+batch: the admitted solves advance round robin (eigenfns_gb300.batched), each one
+request ahead of the host, so the host's work on one solve overlaps the device work
+the others queued, and a request that arrives while others run joins at the next step.
 Solver state (blocks, locked set, operator tables, scratch) stays on the device for
 the life of the request and is released when it finishes. Each solve is the plain
 deflated block LOBPCG of eigenfns_gb300.solver with the same kernels in the same
@@ -96,10 +96,10 @@ def _solve_one(req: SolveRequest, device: torch.device):
 
 
 class EigenServer:
-    """Admission by device-memory footprint; admitted solves run in one lock-step batch."""
+    """Admission by device-memory footprint; admitted solves run in one pipelined batch."""
 
     def __init__(self, budget_bytes: float = 160e9, max_concurrent: int = 16, device=None,
-                 streams: int = 8):
+                 streams: int = 1):
         self.budget = float(budget_bytes)
         self.streams = int(streams)
         self.max_concurrent = int(max_concurrent)

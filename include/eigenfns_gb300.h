@@ -159,10 +159,15 @@ int ef_gram_noalloc(const float* A, const float* B, int ma, int mb, long long K,
 int ef_tune_gram(int ma, int mb, int kernel, int units_per_sm);
 /* drops every ef_tune_gram override */
 int ef_tune_reset(void);
-/* reads and clears the sticky device flag the tensor-core rotation sets when one of its
- * bounded waits ran out (never expected; results of that call are not valid).
+/* reads and clears the sticky device flag the tensor-core Gram and rotation set when one
+ * of their bounded waits ran out (never expected; results of that call are not valid).
  * Synchronises the device. */
 int ef_tc_error(int* flag);
+/* queues a copy of the same flag into *host_flag (pinned host memory) on `stream`,
+ * without clearing it: after the stream reaches the copy, a nonzero value means a
+ * tensor-core kernel queued before it on that stream (or finished before it on another)
+ * timed out. The batch driver reads it per solve without synchronising the device. */
+int ef_tc_error_async(int* host_flag, void* stream);
 /* work bytes of ef_gram_tc for these sizes */
 size_t ef_gram_tc_workspace_bytes(int ma, int mb, long long K);
 /* the Gram of ef_gram (solver.py:35-43) on the tcgen05 tensor cores: 3xTF32 split

@@ -1,6 +1,7 @@
-"""Host logic of the lock-step batch driver (eigenfns_gb300.batched) on the CPU: solves
-of different lengths advance together, one shared transfer per step, failures and a
-tensor-core timeout are reported per solve."""
+"""Host logic of the pipelined batch driver (eigenfns_gb300.batched) on the CPU: solves
+of different lengths advance round robin, each step waits for each solve's own request
+only, failures are reported per solve and a tensor-core timeout fails every solve in
+flight."""
 from __future__ import annotations
 
 import pytest
@@ -8,22 +9,28 @@ import pytest
 torch = pytest.importorskip("torch")
 
 
-class _Stream:
-    def __init__(self, log):
-        self.log = log
-
-    def synchronize(self):
-        self.log.append("sync")
-
-
 @pytest.fixture()
 def driver(monkeypatch):
     from eigenfns_gb300 import batched, blas
     log = []
-    flag = {"tc": 0}
-    monkeypatch.setattr(torch.cuda, "current_stream", lambda d=None: _Stream(log))
+    flag = {"tc": 0, "cleared": 0}
+
+    class _Event:
+        def __init__(self, tag):
+            self.tag = tag
+
+    def clear():
+        flag["cleared"] += 1
+        v, flag["tc"] = flag["tc"], 0
+        return v
+
     monkeypatch.setattr(batched, "_request_to_host", lambda req: req)
-    monkeypatch.setattr(blas, "tc_error", lambda: flag["tc"])
+    monkeypatch.setattr(batched, "_new_flag", lambda: {"v": 0})
+    monkeypatch.setattr(batched, "_queue_flag", lambda f: f.__setitem__("v", flag["tc"]))
+    monkeypatch.setattr(batched, "_flag_value", lambda f: f["v"])
+    monkeypatch.setattr(batched, "_record_event", lambda: _Event(len(log)))
+    monkeypatch.setattr(batched, "_wait", lambda ev: log.append("wait"))
+    monkeypatch.setattr(blas, "tc_error", clear)
     return batched, log, flag
 
 
@@ -38,16 +45,19 @@ def _solve(name, n, log, fail_at=None):
     return name, acc
 
 
-def test_lock_step_shares_one_sync_per_step(driver):
+def test_round_robin_waits_per_solve(driver):
     batched, log, _ = driver
     d = batched.BatchedSolves(streams=1)
     for name, n in (("a", 3), ("b", 1), ("c", 2)):
         d.add(name, _solve(name, n, log))
     out = d.run()
     assert out == {"a": ("a", 3), "b": ("b", 0), "c": ("c", 1)}
-    assert d.steps == 3 and log.count("sync") == 3
-    # every solve queued its step-k work before the step-k synchronisation
-    assert log[:4] == ["a0", "b0", "c0", "sync"]
+    assert d.steps == 3
+    # every solve queued its first request on joining; a step waits for one solve's own
+    # request, resumes it (which queues its next work) and only then waits for the next
+    assert log[:3] == ["a0", "b0", "c0"]
+    assert log[3:9] == ["wait", "a1", "wait", "wait", "c1", "wait"]
+    assert log.count("wait") == 3 + 2 + 1
 
 
 def test_failures_are_per_solve_and_timeouts_fail_all(driver):
@@ -59,8 +69,8 @@ def test_failures_are_per_solve_and_timeouts_fail_all(driver):
     assert out["ok"] == ("ok", 1) and isinstance(out["bad"], ValueError)
     d = batched.BatchedSolves(streams=1)
     d.add("x", _solve("x", 3, log))
+    flag["tc"] = 1                          # a timeout before y's request was copied
     d.add("y", _solve("y", 3, log))
-    flag["tc"] = 1
     out = d.step()
     assert set(out) == {"x", "y"} and all(isinstance(v, RuntimeError) for v in out.values())
-    assert len(d) == 0
+    assert len(d) == 0 and flag["cleared"] == 1 and flag["tc"] == 0

@@ -28,6 +28,10 @@ def fake_server(monkeypatch):
     monkeypatch.setattr(torch.cuda, "synchronize", lambda d=None: None)
     monkeypatch.setattr(torch.cuda, "current_stream", lambda d=None: _Stream())
     monkeypatch.setattr(batched, "_request_to_host", lambda req: req)
+    monkeypatch.setattr(batched, "_new_flag", lambda: [0])
+    monkeypatch.setattr(batched, "_queue_flag", lambda f: None)
+    monkeypatch.setattr(batched, "_record_event", lambda: None)
+    monkeypatch.setattr(batched, "_wait", lambda ev: None)
     monkeypatch.setattr(blas, "tc_error", lambda: 0)
     state = {"running": 0, "peak": 0}
 
