@@ -57,6 +57,14 @@ SIGNATURES = {
     "ef_gram_tc_workspace_bytes": (_sz, [_i, _i, _ll]),
     "ef_tc_error": (_i, [_vp]),
     "ef_tc_error_async": (_i, [_vp, _vp]),
+    "ef_group_theta": (_i, [_vp, _vp, _i, _vp, _ll, _vp, _ll, _i, _vp, _sz, _vp]),
+    "ef_group_precondition": (_i, [_vp, _vp, _i, _vp, _ll, _vp, _ll, _i, _vp, _sz, _vp]),
+    "ef_group_gram": (_i, [_vp, _i, _vp, _ll, _vp, _ll, _i, _i, _ll, _vp, _ll, _vp, _sz, _vp]),
+    "ef_group_rotate": (_i, [_vp, _i, _vp, _ll, _vp, _ll, _vp, _ll, _i, _i, _ll, _i, _vp]),
+    "ef_group_rowstats": (_i, [_vp, _i, _vp, _ll, _vp, _ll, _i, _ll, _vp, _ll, _vp, _sz, _vp]),
+    "ef_group_residual_norms": (_i, [_vp, _i, _vp, _ll, _vp, _ll, _vp, _ll, _vp, _ll, _i, _ll,
+                                     _vp, _ll, _vp, _sz, _vp]),
+    "ef_group_scale_rows": (_i, [_vp, _i, _vp, _ll, _vp, _ll, _i, _ll, _vp]),
     "ef_tune_gram": (_i, [_i, _i, _i, _i]),
     "ef_tune_reset": (_i, []),
     "ef_energy_workspace_bytes": (_i, [_vp, _i]),

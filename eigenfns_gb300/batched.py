@@ -6,7 +6,7 @@ host (residual norms, an SVQB Gram, the Rayleigh-Ritz matrix) and yields those d
 tensors, or a request for the fp64 eigendecomposition of one.
 
 The driver here keeps every active solve one request ahead of the host. When a solve
-yields, its request is copied to pinned host memory on the solve's stream right away,
+yields, its request is copied to pinned host memory on the stream right away,
 followed by a copy of the tensor-core error flag and an event. A step then visits the
 solves in order: it waits for that solve's event only, runs the eigendecomposition on
 the host if one was asked for, and resumes the solve, which queues its next kernels and
@@ -23,12 +23,11 @@ scripts/exp/chain_i6resume.sh).
 """
 from __future__ import annotations
 
-import contextlib
-
 import numpy as np
 import torch
 
-from . import blas
+from . import blas, hosteig
+from .grouped import GroupResults
 from .solver import HostEigh, lobpcg_steps
 
 
@@ -57,7 +56,8 @@ def _request_to_host(req):
 def _host_data(h):
     """What the solve is sent back: numpy copies, or the fp64 eigh it asked for."""
     if isinstance(h, _EighOnHost):
-        return np.linalg.eigh(h.A.numpy())
+        A = h.A.numpy()
+        return hosteig.eigh_many(A) if A.ndim == 3 else hosteig.eigh(A)
     if isinstance(h, tuple):
         return tuple(x.numpy() for x in h)
     return h.numpy()
@@ -95,17 +95,14 @@ class _Pending:
 class BatchedSolves:
     """Pipelined round-robin driver of step generators.
 
-    `streams` > 1 binds each solve to one of that many CUDA streams (round robin as solves
-    join), so that the small kernels of different solves may also run side by side on
-    the device; each solve's own kernels keep their order and its scratch buffers are
-    per stream. With 1 (the default) every solve queues on the caller's stream."""
+    Every solve queues on the caller's stream, so the device runs the solves' work in
+    the order the host issued it. (Binding solves to separate streams let small kernels
+    of different solves overlap, 7 % faster on the 24-solve mix, but changed some solves'
+    iteration counts against the solve run alone, so it is not offered.)"""
 
-    def __init__(self, streams: int = 1):
+    def __init__(self):
         self._active: dict = {}     # key -> _Pending
-        self._stream_of: dict = {}
         self._flags: dict = {}
-        self._streams = [torch.cuda.Stream() for _ in range(streams)] if streams > 1 else None
-        self._next = 0
         self.steps = 0
 
     def __len__(self) -> int:
@@ -114,44 +111,45 @@ class BatchedSolves:
     def keys(self):
         return list(self._active)
 
-    def _ctx(self, key):
-        if self._streams is None:
-            return contextlib.nullcontext()
-        return torch.cuda.stream(self._stream_of[key])
-
     def _queue(self, key, gen, req) -> None:
         """Copy the request, then the error flag, to the host behind the solve's work."""
-        with self._ctx(key):
-            host = _request_to_host(req)
-            flag = self._flags[key]
-            _queue_flag(flag)
-            ev = _record_event()
-        self._active[key] = _Pending(gen, host, ev, flag)
+        host = _request_to_host(req)
+        flag = self._flags[key]
+        _queue_flag(flag)
+        self._active[key] = _Pending(gen, host, _record_event(), flag)
 
     def _drop(self, key) -> None:
         self._active.pop(key, None)
         self._flags.pop(key, None)
-        s = self._stream_of.pop(key, None)
-        if s is not None:                       # results are used on the caller's stream
-            torch.cuda.current_stream().wait_stream(s)
+
+    def _advance(self, key, gen, data, finished: dict, first: bool = False) -> None:
+        """Resume a solve with `data` up to its next host read and queue that read; results
+        of group members reported on the way go to `finished`."""
+        try:
+            req = next(gen) if first else gen.send(data)
+            while isinstance(req, GroupResults):
+                finished.update(req.results)
+                req = gen.send(None)
+        except StopIteration as stop:
+            if isinstance(stop.value, GroupResults):
+                finished.update(stop.value.results)
+            else:
+                finished[key] = stop.value
+            self._drop(key)
+            return
+        except Exception as exc:            # surfaced to the caller per solve (or group)
+            finished[key] = exc
+            self._drop(key)
+            return
+        self._queue(key, gen, req)
 
     def add(self, key, gen) -> dict:
-        """Start a solve (runs it up to its first host read). Returns {key: result} if it
-        finished without reading anything (never for LOBPCG)."""
-        if self._streams is not None:
-            self._stream_of[key] = self._streams[self._next % len(self._streams)]
-            self._next += 1
-            # the solve's inputs were made on the caller's stream
-            self._stream_of[key].wait_stream(torch.cuda.current_stream())
+        """Start a solve (runs it up to its first host read). Returns what finished without
+        reading anything ({key: result}; never for LOBPCG)."""
         self._flags[key] = _new_flag()
-        try:
-            with self._ctx(key):
-                req = next(gen)
-        except StopIteration as stop:
-            self._drop(key)
-            return {key: stop.value}
-        self._queue(key, gen, req)
-        return {}
+        finished: dict = {}
+        self._advance(key, gen, None, finished, first=True)
+        return finished
 
     def _fail_all(self, finished: dict) -> None:
         # a tensor-core pipeline wait ran out: every solve in flight may hold invalid data
@@ -174,17 +172,7 @@ class BatchedSolves:
             if _flag_value(p.flag):
                 self._fail_all(finished)
                 break
-            try:
-                data = _host_data(p.host)
-                with self._ctx(k):
-                    req = p.gen.send(data)
-                self._queue(k, p.gen, req)
-            except StopIteration as stop:
-                finished[k] = stop.value
-                self._drop(k)
-            except Exception as exc:            # surfaced to the caller per solve
-                finished[k] = exc
-                self._drop(k)
+            self._advance(k, p.gen, _host_data(p.host), finished)
         self.steps += 1
         return finished
 
@@ -196,27 +184,56 @@ class BatchedSolves:
         return out
 
 
+def group_by_shape(ops, ms, guards, max_group: int = 64) -> list:
+    """Instances that can share a group (same grid edge, device, block and guard), in
+    input order, split into groups of at most max_group: [[instance index, ...], ...]."""
+    groups: dict = {}
+    for i, op in enumerate(ops):
+        groups.setdefault((op.grid_size, str(op.device), int(ms[i]), int(guards[i])), []).append(i)
+    out = []
+    for members in groups.values():
+        out.extend(members[s:s + max_group] for s in range(0, len(members), max_group))
+    return out
+
+
 def lobpcg_batched(ops, nevs, m: int = 32, guard: int = 8, tol: float = 1e-4, maxit: int = 400,
-                   seeds=None, streams: int = 1, **kw) -> list:
-    """Solve several operators' lowest eigenpairs, interleaved.
+                   seeds=None, grouped: bool = True, max_group: int = 64, **kw) -> list:
+    """Solve several operators' lowest eigenpairs together.
 
     `ops` are MaxwellOperators (any mix of grids and k-points), `nevs` the bands wanted
     from each (an int applies to all); `m`/`guard` may also be per-instance lists.
-    Returns [(eigenvalues, locked vectors, SolveStats)] in the order of `ops`, each equal
-    to lobpcg_blocks(op, nev, ...) run alone; raises the first failure after the batch.
-    `streams` CUDA streams are shared round robin by the solves (1: the current stream).
+    With `grouped` (the default) the instances of one shape run as grouped solves
+    (eigenfns_gb300.grouped: one launch sequence per iteration for the whole group), the
+    groups interleaved by the pipelined driver; otherwise every instance is its own
+    interleaved solve. Returns [(eigenvalues, locked vectors, SolveStats)] in the order
+    of `ops`, each equal to lobpcg_blocks(op, nev, ...) run alone; raises the first
+    failure after the batch.
     """
+    from .grouped import lobpcg_group_steps
     n = len(ops)
     per = lambda v: list(v) if isinstance(v, (list, tuple)) else [v] * n
     nevs, ms, guards = per(nevs), per(m), per(guard)
     seeds = per(0 if seeds is None else seeds)
-    drv = BatchedSolves(streams)
-    out = {}
-    for i, op in enumerate(ops):
-        out.update(drv.add(i, lobpcg_steps(op, nevs[i], m=ms[i], guard=guards[i], tol=tol,
-                                           maxit=maxit, seed=seeds[i], verbose=False,
-                                           check_tc=False, **kw)))
+    drv = BatchedSolves()
+    out: dict = {}
+    members: dict = {}
+    if grouped:
+        for g, idx in enumerate(group_by_shape(ops, ms, guards, max_group)):
+            members[("group", g)] = idx
+            i0 = idx[0]
+            out.update(drv.add(("group", g), lobpcg_group_steps(
+                [ops[i] for i in idx], [nevs[i] for i in idx], keys=idx, m=ms[i0], guard=guards[i0],
+                tol=tol, maxit=maxit, seeds=[seeds[i] for i in idx], **kw)))
+    else:
+        for i, op in enumerate(ops):
+            out.update(drv.add(i, lobpcg_steps(op, nevs[i], m=ms[i], guard=guards[i], tol=tol,
+                                               maxit=maxit, seed=seeds[i], verbose=False,
+                                               check_tc=False, **kw)))
     out.update(drv.run())
+    for gk, idx in members.items():          # a group that failed as a whole
+        if gk in out:
+            for i in idx:
+                out.setdefault(i, out[gk])
     res = [out[i] for i in range(n)]
     for r in res:
         if isinstance(r, Exception):

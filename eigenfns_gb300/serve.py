@@ -98,10 +98,8 @@ def _solve_one(req: SolveRequest, device: torch.device):
 class EigenServer:
     """Admission by device-memory footprint; admitted solves run in one pipelined batch."""
 
-    def __init__(self, budget_bytes: float = 160e9, max_concurrent: int = 16, device=None,
-                 streams: int = 1):
+    def __init__(self, budget_bytes: float = 160e9, max_concurrent: int = 16, device=None):
         self.budget = float(budget_bytes)
-        self.streams = int(streams)
         self.max_concurrent = int(max_concurrent)
         self.device = torch.device(device) if device is not None else torch.device(
             "cuda", torch.cuda.current_device())
@@ -120,7 +118,7 @@ class EigenServer:
                 raise ValueError(f"request {r.rid} needs {footprint_bytes(r) / 1e9:.1f} GB, "
                                  f"above the {self.budget / 1e9:.1f} GB budget")
         results: list = []
-        batch = BatchedSolves(self.streams if self.device.type == "cuda" else 1)
+        batch = BatchedSolves()
         running: dict = {}            # rid -> (request, footprint, start, operator)
         t0 = time.perf_counter()
 

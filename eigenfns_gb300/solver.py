@@ -59,10 +59,11 @@ def svqb_from_eig(w: np.ndarray, V: np.ndarray, drop: float = _SVQB_DROP):
 
 
 class HostEigh:
-    """A step generator's request for numpy.linalg.eigh of a Hermitian device matrix.
+    """A step generator's request for the fp64 eigendecomposition (numpy.linalg.eigh
+    convention) of a Hermitian device matrix, or of a stack (b, n, n) of them.
 
-    The driver returns (w, V). Single solves (run_steps) run it in place; the batched
-    driver runs the requests of all solves in a step in parallel host threads."""
+    The driver returns (w, V), stacked for a stack (eigenfns_gb300.hosteig: single-
+    threaded LAPACK per problem, the problems of a stack on parallel host threads)."""
     __slots__ = ("A",)
 
     def __init__(self, A: torch.Tensor):
@@ -141,7 +142,9 @@ def _ortho_inplace(X: torch.Tensor, passes: int = 2, drop: float = _SVQB_DROP) -
 
 def _to_host(req):
     if isinstance(req, HostEigh):
-        return np.linalg.eigh(req.A.cpu().numpy())
+        from . import hosteig
+        A = req.A.cpu().numpy()
+        return hosteig.eigh_many(A) if A.ndim == 3 else hosteig.eigh(A)
     if isinstance(req, tuple):
         return tuple(t.cpu().numpy() for t in req)
     return req.cpu().numpy()

@@ -238,6 +238,39 @@ int ef_rand_block(const ef_op* op, float* X, int m, uint64_t seed, uint64_t stre
 /* X *= mask(kn > 0) */
 int ef_apply_mask(const ef_op* op, float* X, int m, void* stream);
 
+/* ---- grouped block operations (no counterpart in the reference) ------------------ */
+/* The same operation on the blocks of several instances of one shape (one grid edge and
+ * block size; any k-point or structure) in one call: instance i's operand starts at
+ * base + i * stride, where strides count complex64 values for vector blocks and
+ * coefficient matrices, complex128 entries for Gram outputs and doubles for row
+ * statistics, eigenvalues, squared norms and scales; inst[0..n) (host memory) lists the
+ * instances covered. Each instance's work is the single-instance call on its operands
+ * (so results equal the instance computed alone), queued in list order on `stream` with
+ * one workspace sized for one instance. Replaces, per instance, the calls of
+ * eigenfns/operator.py:82-95 / 104-127 and eigenfns/solver.py:35-57, 228-238. */
+int ef_group_theta(const ef_op* const* ops, const int* inst, int n, const float* X,
+                   long long x_stride, float* Y, long long y_stride, int m, void* work,
+                   size_t work_bytes, void* stream);
+int ef_group_precondition(const ef_op* const* ops, const int* inst, int n, const float* X,
+                          long long x_stride, float* Y, long long y_stride, int m, void* work,
+                          size_t work_bytes, void* stream);
+int ef_group_gram(const int* inst, int n, const float* A, long long a_stride, const float* B,
+                  long long b_stride, int ma, int mb, long long K, double* G, long long g_stride,
+                  void* work, size_t work_bytes, void* stream);
+int ef_group_rotate(const int* inst, int n, const float* C, long long c_stride, const float* S,
+                    long long s_stride, float* out, long long o_stride, int m_in, int m_out,
+                    long long K, int mode, void* stream);
+int ef_group_rowstats(const int* inst, int n, const float* A, long long a_stride, const float* B,
+                      long long b_stride, int m, long long K, double* out, long long out_stride,
+                      void* work, size_t work_bytes, void* stream);
+int ef_group_residual_norms(const int* inst, int n, const float* HX, long long h_stride,
+                            const float* X, long long x_stride, const double* lam,
+                            long long lam_stride, float* R, long long r_stride, int m, long long K,
+                            double* r2, long long r2_stride, void* work, size_t work_bytes,
+                            void* stream);
+int ef_group_scale_rows(const int* inst, int n, float* X, long long x_stride, const double* scale,
+                        long long s_stride, int m, long long K, void* stream);
+
 /* ---- benchmark inputs (no counterpart in the reference) -------------------------- */
 /* eps of a periodic rod network averaged over sub^3 sub-samples per voxel into
  * eps_host (G^3 float32, host). rods_host is (n_rods, 7) float64: endpoints p, q

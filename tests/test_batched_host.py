@@ -47,7 +47,7 @@ def _solve(name, n, log, fail_at=None):
 
 def test_round_robin_waits_per_solve(driver):
     batched, log, _ = driver
-    d = batched.BatchedSolves(streams=1)
+    d = batched.BatchedSolves()
     for name, n in (("a", 3), ("b", 1), ("c", 2)):
         d.add(name, _solve(name, n, log))
     out = d.run()
@@ -62,15 +62,58 @@ def test_round_robin_waits_per_solve(driver):
 
 def test_failures_are_per_solve_and_timeouts_fail_all(driver):
     batched, log, flag = driver
-    d = batched.BatchedSolves(streams=1)
+    d = batched.BatchedSolves()
     d.add("ok", _solve("ok", 2, log))
     d.add("bad", _solve("bad", 3, log, fail_at=0))
     out = d.run()
     assert out["ok"] == ("ok", 1) and isinstance(out["bad"], ValueError)
-    d = batched.BatchedSolves(streams=1)
+    d = batched.BatchedSolves()
     d.add("x", _solve("x", 3, log))
     flag["tc"] = 1                          # a timeout before y's request was copied
     d.add("y", _solve("y", 3, log))
     out = d.step()
     assert set(out) == {"x", "y"} and all(isinstance(v, RuntimeError) for v in out.values())
     assert len(d) == 0 and flag["cleared"] == 1 and flag["tc"] == 0
+
+
+def _group(names, lengths, log):
+    """A stand-in grouped solve: members finish after their own number of steps and are
+    reported through GroupResults at the step they finish."""
+    from eigenfns_gb300.grouped import GroupResults
+    left = dict(zip(names, lengths))
+    step = 0
+    while True:
+        log.append(f"g{step}")
+        yield torch.tensor([float(step)])
+        step += 1
+        done = {k: (k, step) for k, n in left.items() if n == step}
+        for k in done:
+            del left[k]
+        if not left:
+            return GroupResults(done)
+        if done:
+            yield GroupResults(done)
+
+
+def test_group_members_report_as_they_finish(driver):
+    batched, log, _ = driver
+    d = batched.BatchedSolves()
+    d.add(("group", 0), _group(["p", "q", "r"], [1, 3, 2], log))
+    d.add("solo", _solve("solo", 2, log))
+    seen = []
+    while len(d):
+        seen.append(sorted(map(str, d.step())))
+    assert seen == [["p"], ["r", "solo"], ["q"]]
+
+
+def test_group_by_shape_keeps_order_and_caps_size():
+    from eigenfns_gb300.batched import group_by_shape
+
+    class _Op:
+        def __init__(self, g):
+            self.grid_size, self.device = g, "cuda:0"
+
+    ops = [_Op(g) for g in (32, 48, 32, 32, 48, 32)]
+    ms = [16, 32, 16, 16, 32, 8]
+    groups = group_by_shape(ops, ms, [4] * 6, max_group=2)
+    assert groups == [[0, 2], [3], [1, 4], [5]]

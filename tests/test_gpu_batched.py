@@ -35,3 +35,41 @@ def test_batched_equals_alone():
         assert np.abs(va - vb).max() <= 1e-12 * np.abs(va).max()
         assert sa.iterations == sb.iterations
         assert torch.equal(xa, xb)
+
+
+def test_batched_one_at_a_time_equals_alone():
+    """The same instances as interleaved single solves (no grouping)."""
+    from eigenfns_gb300.batched import lobpcg_batched
+    from eigenfns_gb300.solver import lobpcg_blocks
+    inst = _instances()[:2]
+    alone = [lobpcg_blocks(op, nev, m=m, guard=g, tol=1e-4, seed=s, verbose=False)
+             for op, nev, m, g, s in inst]
+    batch = lobpcg_batched([i[0] for i in inst], [i[1] for i in inst], m=[i[2] for i in inst],
+                           guard=[i[3] for i in inst], tol=1e-4, seeds=[i[4] for i in inst],
+                           grouped=False)
+    for (va, xa, sa), (vb, xb, sb) in zip(alone, batch):
+        assert np.array_equal(va, vb) and sa.iterations == sb.iterations
+        assert torch.equal(xa, xb)
+
+
+def test_grouped_members_equal_alone():
+    """One group (32^3, block 12, guard 4) of members with different k-points, seeds and
+    band counts (1 to 3 blocks each): every member's eigenvalues, locked vectors,
+    iteration counts and Θ-application counts equal its solve run alone."""
+    from eigenfns_gb300.grouped import lobpcg_grouped
+    from eigenfns_gb300.operator import MaxwellOperator
+    from eigenfns_gb300.solver import lobpcg_blocks
+    from eigenfns_gb300.structure import bz_kpoint, make_structure
+    ops, nevs, seeds = [], [12, 8, 20, 16], [11, 12, 13, 14]
+    for s in seeds:
+        eps, L, _ = make_structure(64, 32, seed=s)
+        ops.append(MaxwellOperator(eps, L, k_frac=bz_kpoint(s)))
+    alone = [lobpcg_blocks(op, nev, m=12, guard=4, tol=1e-4, seed=s, verbose=False)
+             for op, nev, s in zip(ops, nevs, seeds)]
+    group = lobpcg_grouped(ops, nevs, m=12, guard=4, tol=1e-4, seeds=seeds)
+    for (va, xa, sa), (vb, xb, sb) in zip(alone, group):
+        assert np.array_equal(va, vb)
+        assert torch.equal(xa, xb)
+        assert sa.iterations == sb.iterations
+        assert sa.theta_applications == sb.theta_applications
+        assert [r["iters"] for r in sa.rounds] == [r["iters"] for r in sb.rounds]
