@@ -324,7 +324,7 @@ BATCHED_KINDS = ((64, 32, 16, 16, 4), (216, 48, 32, 32, 8), (512, 64, 48, 32, 8)
 
 
 def _batched_instances(dev, seeds_per_kind: int) -> dict:
-    """The 48-instance batched workload: one lock-step batch against one-at-a-time solves."""
+    """The 48-instance batched workload: grouped solves against one-at-a-time solves."""
     import numpy as np
     import torch
     from eigenfns_gb300.batched import lobpcg_batched
@@ -479,8 +479,9 @@ def run_ours(args, w):
 
     # served vs plain: a seeded Poisson stream of smaller eigensolve requests (N in
     # {64, 216, 512} on 32^3/48^3/64^3, random Bloch k, 8-48 bands) solved by the
-    # continuously batched server (device-memory admission, lock-step batch) and by
-    # the plain one-at-a-time path
+    # continuously batched server (device-memory admission, requests of one shape started
+    # as grouped solves, groups interleaved by the pipelined driver) and by the plain
+    # one-at-a-time path; both build each request's structure and operator
     served = None
     if not args.no_served:
         from eigenfns_gb300.serve import EigenServer, poisson_requests, run_plain, summarize
@@ -498,11 +499,13 @@ def run_ours(args, w):
         served = {"workload": f"{len(reqs)} Poisson requests (40/s): N in (64, 216, 512) on 32^3/48^3/64^3, "
                               "random k, 8-48 bands, tol 1e-4; 160 GB admission budget, 32 slots",
                   "served": ss, "plain": sp, "speedup": ss["modes_per_s"] / sp["modes_per_s"],
-                  "peak_concurrent": srv.peak_concurrent, "max_rel_diff_served_vs_plain": same}
+                  "peak_concurrent": srv.peak_concurrent, "groups": srv.groups,
+                  "max_rel_diff_served_vs_plain": same}
 
     # batched launch of 48 uneven instances: rod networks with N in {64, 216, 512} (16 seeds
     # each) on 32^3/48^3/64^3, a k-point drawn in each supercell's first Brillouin zone,
-    # 16/32/48 lowest bands; all solved in one lock-step batch against one at a time
+    # 16/32/48 lowest bands; solved as grouped solves (one per shape, interleaved)
+    # against one at a time
     batched = None
     if not args.no_batched:
         batched = _batched_instances(dev, args.batched_seeds)

@@ -1,15 +1,18 @@
 """A continuously batched eigensolve server on one GPU.
 
 Requests (structure seed and size, grid, Bloch k, number of bands, tolerance)
-arrive over time. The server admits a waiting request as soon as a slot is free
-and its device-memory footprint fits the budget, and adds its solve to the running
-batch: the admitted solves advance round robin (eigenfns_gb300.batched), each one
-request ahead of the host, so the host's work on one solve overlaps the device work
-the others queued, and a request that arrives while others run joins at the next step.
-Solver state (blocks, locked set, operator tables, scratch) stays on the device for
-the life of the request and is released when it finishes. Each solve is the plain
-deflated block LOBPCG of eigenfns_gb300.solver with the same kernels in the same
-order as alone, so its result is the same alone and in the mix.
+arrive over time. The server admits waiting requests when slots are free and their
+device-memory footprints fit the budget. Admitted requests of one shape (grid edge and
+LOBPCG block) start together as one grouped solve (eigenfns_gb300.grouped: one launch
+sequence per iteration for the whole group, their projected problems on parallel host
+threads); all running groups advance round robin in the pipelined batch driver
+(eigenfns_gb300.batched), so the host's work on one group overlaps the device work of
+the others. While the GPU is busy, newly arrived requests wait up to `group_wait`
+seconds (or until `min_group` of them are waiting) so that they start as a group rather
+than one by one. A request's result is reported when its own bands are locked; a
+group's device memory is released when its last member finishes. Each member computes
+exactly what its solve computes alone (grouped solves are bit-for-bit the single
+solves), so a request's result is the same served and plain.
 
 `run_plain` processes the same requests one at a time (the plain path) for the
 served-vs-plain comparison.
@@ -37,10 +40,11 @@ class SolveRequest:
     arrival: float = 0.0          # seconds after the start of the run
 
     def block(self) -> tuple:
-        """LOBPCG block and guard for this request: about nev/2 per block, 8..32."""
-        m = int(min(32, max(8, 2 * math.ceil(self.nev / 4))))
-        guard = max(2, m // 4)
-        return m, guard
+        """LOBPCG block and guard for this request: 8, 16, 24 or 32 vectors (about half
+        the bands per block, rounded up to a multiple of 8 so that requests share shapes),
+        guard a quarter of the block."""
+        m = int(min(32, 8 * math.ceil(self.nev / 16)))
+        return m, m // 4
 
 
 @dataclass
@@ -87,6 +91,18 @@ def _steps(req: SolveRequest, op, check_tc: bool):
                         verbose=False, check_tc=check_tc)
 
 
+def _shape(req: SolveRequest) -> tuple:
+    return (req.grid,) + req.block() + (req.tol,)
+
+
+def _group_steps(reqs: list, ops: list):
+    """One grouped solve for requests of one shape (members keyed by request id)."""
+    from .grouped import lobpcg_group_steps
+    m, guard = reqs[0].block()
+    return lobpcg_group_steps(ops, [r.nev for r in reqs], keys=[r.rid for r in reqs], m=m,
+                              guard=guard, tol=reqs[0].tol, seeds=[r.seed for r in reqs])
+
+
 def _solve_one(req: SolveRequest, device: torch.device):
     from .solver import run_steps
     op = _operator(req, device)
@@ -96,11 +112,16 @@ def _solve_one(req: SolveRequest, device: torch.device):
 
 
 class EigenServer:
-    """Admission by device-memory footprint; admitted solves run in one pipelined batch."""
+    """Admission by device-memory footprint; admitted requests of one shape start as one
+    grouped solve; the running groups advance in one pipelined batch."""
 
-    def __init__(self, budget_bytes: float = 160e9, max_concurrent: int = 16, device=None):
+    def __init__(self, budget_bytes: float = 160e9, max_concurrent: int = 16, device=None,
+                 group_wait: float = 0.1, min_group: int = 4, max_group: int = 32):
         self.budget = float(budget_bytes)
         self.max_concurrent = int(max_concurrent)
+        self.group_wait = float(group_wait)
+        self.min_group = int(min_group)
+        self.max_group = int(max_group)
         self.device = torch.device(device) if device is not None else torch.device(
             "cuda", torch.cuda.current_device())
         self._used = 0.0
@@ -108,6 +129,7 @@ class EigenServer:
         self.peak_used = 0.0
         self.errors: list = []
         self.steps = 0
+        self.groups = 0
 
     def run(self, requests, realtime: bool = True) -> list:
         """Serve `requests` (arrival times honoured when `realtime`); returns results."""
@@ -119,40 +141,72 @@ class EigenServer:
                                  f"above the {self.budget / 1e9:.1f} GB budget")
         results: list = []
         batch = BatchedSolves()
-        running: dict = {}            # rid -> (request, footprint, start, operator)
+        running: dict = {}            # rid -> (request, start, group key)
+        groups: dict = {}             # group key -> [members still running, bytes held]
         t0 = time.perf_counter()
 
-        def finish(done: dict):
-            for rid, res in done.items():
-                req, fp, start, _ = running.pop(rid)
-                self._used -= fp
-                if isinstance(res, Exception):
-                    self.errors.append((rid, repr(res)))
-                    continue
+        def record(rid, res):
+            req, start, gk = running.pop(rid)
+            if isinstance(res, Exception):
+                self.errors.append((rid, repr(res)))
+            else:
                 vals, vecs, st = res
                 del vecs
                 results.append(SolveResult(rid, vals, max(r["max_res_locked"] for r in st.rounds),
                                            req.arrival, start, time.perf_counter() - t0,
                                            st.theta_applications, st.iterations))
+            g = groups[gk]
+            g[0] -= 1
+            if g[0] == 0:                 # the group's stacked arrays are gone
+                self._used -= g[1]
+                del groups[gk]
+
+        def finish(done: dict):
+            for key, res in done.items():
+                if key in groups:         # the grouped solve failed as a whole
+                    for rid in [r for r, v in running.items() if v[2] == key]:
+                        record(rid, res)
+                elif key in running:
+                    record(key, res)
+
+        def admit(now):
+            """Take arrived requests that fit (slots, memory) and start them as groups."""
+            take = []
+            while pending:
+                head = pending[0]
+                fp = footprint_bytes(head)
+                arrived = (not realtime) or head.arrival <= now
+                if not (arrived and len(running) + len(take) < self.max_concurrent
+                        and self._used + fp <= self.budget):
+                    break
+                pending.pop(0)
+                self._used += fp
+                take.append((head, fp))
+            by_shape: dict = {}
+            for req, fp in take:
+                by_shape.setdefault(_shape(req), []).append((req, fp))
+            for members in by_shape.values():
+                for c in range(0, len(members), self.max_group):
+                    chunk = members[c:c + self.max_group]
+                    gk = ("group", self.groups)
+                    self.groups += 1
+                    start = time.perf_counter() - t0
+                    reqs = [r for r, _ in chunk]
+                    ops = [_operator(r, self.device) for r in reqs]
+                    groups[gk] = [len(reqs), float(sum(fp for _, fp in chunk))]
+                    for r in reqs:
+                        running[r.rid] = (r, start, gk)
+                    finish(batch.add(gk, _group_steps(reqs, ops)))
+            self.peak_concurrent = max(self.peak_concurrent, len(running))
+            self.peak_used = max(self.peak_used, self._used)
 
         with torch.cuda.device(self.device):
             while pending or len(batch):
                 now = time.perf_counter() - t0
-                while pending:
-                    head = pending[0]
-                    fp = footprint_bytes(head)
-                    arrived = (not realtime) or head.arrival <= now
-                    if not (arrived and len(running) < self.max_concurrent
-                            and self._used + fp <= self.budget):
-                        break
-                    pending.pop(0)
-                    self._used += fp
-                    start = time.perf_counter() - t0
-                    op = _operator(head, self.device)
-                    running[head.rid] = (head, fp, start, op)
-                    self.peak_concurrent = max(self.peak_concurrent, len(running))
-                    self.peak_used = max(self.peak_used, self._used)
-                    finish(batch.add(head.rid, _steps(head, op, False)))
+                waiting = [r for r in pending[:self.min_group] if (not realtime) or r.arrival <= now]
+                if waiting and (not running or len(waiting) >= self.min_group
+                                or now - waiting[0].arrival >= self.group_wait):
+                    admit(now)
                 if len(batch):
                     finish(batch.step())
                 elif pending and realtime:

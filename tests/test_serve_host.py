@@ -63,8 +63,39 @@ def fake_server(monkeypatch):
         vals, _, st = run_steps(fake_steps(req, None, True))
         return vals, st
 
+    def fake_group(reqs, ops):
+        """Members advance in lock step on one shared host read; each is reported as
+        it finishes, as the grouped solver does."""
+        from eigenfns_gb300.grouped import GroupResults
+        gens, done = {}, {}
+        for r in reqs:
+            g = fake_steps(r, None, False)
+            try:
+                next(g)
+                gens[r.rid] = g
+            except StopIteration as stop:
+                done[r.rid] = stop.value
+        while gens:
+            h = yield torch.zeros(2)
+            finished = {}
+            for rid, g in list(gens.items()):
+                try:
+                    g.send(h)
+                except StopIteration as stop:
+                    finished[rid] = stop.value
+                    del gens[rid]
+                except Exception as exc:
+                    finished[rid] = exc
+                    del gens[rid]
+            done.update(finished)
+            if finished and gens:
+                yield GroupResults(finished)
+                done = {}
+        return GroupResults(done)
+
     monkeypatch.setattr(serve, "_operator", lambda req, device: None)
     monkeypatch.setattr(serve, "_steps", fake_steps)
+    monkeypatch.setattr(serve, "_group_steps", fake_group)
     monkeypatch.setattr(serve, "_solve_one", fake_solve)
     return serve, state
 
@@ -122,3 +153,13 @@ def test_request_stream_is_seeded():
     assert all(a[i].arrival < a[i + 1].arrival for i in range(19))
     assert all(-0.5 <= x < 0.5 for r in a for x in r.k_frac)
     assert all(8 <= r.nev <= 48 and r.grid in (32, 48, 64) for r in a)
+
+
+def test_waiting_requests_start_as_groups(fake_server):
+    serve, _ = fake_server
+    reqs = [serve.SolveRequest(rid=i, nodes=64, grid=32 if i < 6 else 48, seed=100 + i,
+                               nev=12 if i % 2 else 30, arrival=0.0) for i in range(10)]
+    srv = serve.EigenServer(budget_bytes=1e15, max_concurrent=16, device="cpu")
+    res = srv.run(reqs, realtime=False)
+    # one group per (grid, block) shape: 32^3 x {8, 16} and 48^3 x {8, 16}
+    assert len(res) == 10 and srv.groups == 4 and srv.peak_concurrent == 10
