@@ -39,12 +39,12 @@ class SolveRequest:
     tol: float = 1e-4
     arrival: float = 0.0          # seconds after the start of the run
 
+    block_size: int = 16          # LOBPCG block; the guard is a quarter of it
+
     def block(self) -> tuple:
-        """LOBPCG block and guard for this request: 8, 16, 24 or 32 vectors (about half
-        the bands per block, rounded up to a multiple of 8 so that requests share shapes),
-        guard a quarter of the block."""
-        m = int(min(32, 8 * math.ceil(self.nev / 16)))
-        return m, m // 4
+        """LOBPCG block and guard: one block size for every request by default, so that
+        requests on one grid share a shape and can run as one grouped solve."""
+        return int(self.block_size), int(self.block_size) // 4
 
 
 @dataclass
@@ -116,7 +116,7 @@ class EigenServer:
     grouped solve; the running groups advance in one pipelined batch."""
 
     def __init__(self, budget_bytes: float = 160e9, max_concurrent: int = 16, device=None,
-                 group_wait: float = 0.1, min_group: int = 4, max_group: int = 32):
+                 group_wait: float = 0.3, min_group: int = 8, max_group: int = 32):
         self.budget = float(budget_bytes)
         self.max_concurrent = int(max_concurrent)
         self.group_wait = float(group_wait)

@@ -1,8 +1,9 @@
 """The request server: concurrent solves give the same results as solving alone.
 
-Each solve runs the same deterministic kernels on its own stream, so the
-eigenvalues served in a mix must equal those of the plain one-at-a-time path
-(compared at 1e-12 relative, i.e. bit-for-bit up to host LAPACK threading).
+Requests of one shape run as one grouped solve, whose members run the same
+deterministic kernels and host arithmetic as their solves alone, so the eigenvalues
+served in a mix must equal those of the plain one-at-a-time path (compared at 1e-12
+relative; they agree bit for bit).
 """
 from __future__ import annotations
 
@@ -70,3 +71,24 @@ def test_footprint_covers_measured_device_memory():
         torch.cuda.synchronize()
         used = torch.cuda.max_memory_allocated() - base
         assert used <= footprint_bytes(req), (used, footprint_bytes(req))
+
+
+def test_group_footprint_covers_measured_device_memory():
+    """A grouped solve's device memory (stacked slabs, locked sets, temporaries) stays
+    within the sum of its members' admission footprints."""
+    from eigenfns_gb300 import blas
+    from eigenfns_gb300.grouped import run_group
+    from eigenfns_gb300.serve import SolveRequest, _group_steps, _operator, footprint_bytes
+    reqs = [SolveRequest(i, 216, 48, 30 + i, 24, (0.1 * i, 0.0, -0.1)) for i in range(3)]
+    dev = torch.device("cuda", 0)
+    ops = [_operator(r, dev) for r in reqs]
+    blas.release_workspaces()
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    base = torch.cuda.memory_allocated()
+    torch.cuda.reset_peak_memory_stats()
+    res = run_group(_group_steps(reqs, ops))
+    torch.cuda.synchronize()
+    used = torch.cuda.max_memory_allocated() - base
+    assert sorted(res) == [0, 1, 2] and not any(isinstance(v, Exception) for v in res.values())
+    assert used <= sum(footprint_bytes(r) for r in reqs), (used, [footprint_bytes(r) for r in reqs])

@@ -158,7 +158,8 @@ def test_request_stream_is_seeded():
 def test_waiting_requests_start_as_groups(fake_server):
     serve, _ = fake_server
     reqs = [serve.SolveRequest(rid=i, nodes=64, grid=32 if i < 6 else 48, seed=100 + i,
-                               nev=12 if i % 2 else 30, arrival=0.0) for i in range(10)]
+                               nev=12 if i % 2 else 30, arrival=0.0,
+                               block_size=8 if i in (0, 6) else 16) for i in range(10)]
     srv = serve.EigenServer(budget_bytes=1e15, max_concurrent=16, device="cpu")
     res = srv.run(reqs, realtime=False)
     # one group per (grid, block) shape: 32^3 x {8, 16} and 48^3 x {8, 16}
