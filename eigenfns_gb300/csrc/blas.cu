@@ -399,9 +399,12 @@ __global__ void __launch_bounds__(RK_T) rotate_tiled_kernel(const float2* __rest
 
 // ---- per-row statistics ----------------------------------------------------------
 // For each row i: <A_i, B_i> (complex), |A_i|^2, |B_i|^2. Products in fp32, runs of
-// 32 float4 loads flushed into fp64, chunks reduced in fp64 in a fixed order.
+// 32 float4 loads flushed into fp64, chunks reduced in fp64 in a fixed order. SAME: B is
+// A (row norms of one block): each value is loaded once and used as both operands, the
+// same arithmetic on half the traffic.
 constexpr int DTHREADS = 256;
 
+template <bool SAME>
 __global__ void __launch_bounds__(DTHREADS) rowstats_kernel(const float4* __restrict__ A,
                                                             const float4* __restrict__ B,
                                                             long long K2, long long kchunk,
@@ -426,11 +429,11 @@ __global__ void __launch_bounds__(DTHREADS) rowstats_kernel(const float4* __rest
         long long k = k0 + ((long long)r * U + u) * blockDim.x + threadIdx.x;
         bool ok = k < ke;
         x[u] = ok ? a[k] : make_float4(0.f, 0.f, 0.f, 0.f);
-        y[u] = ok ? b[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (!SAME) y[u] = ok ? b[k] : make_float4(0.f, 0.f, 0.f, 0.f);
       }
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        float4 p = x[u], q = y[u];
+        float4 p = x[u], q = SAME ? x[u] : y[u];
         f[0] = fmaf(p.x, q.x, fmaf(p.y, q.y, fmaf(p.z, q.z, fmaf(p.w, q.w, f[0]))));
         f[1] = fmaf(p.x, q.y, fmaf(-p.y, q.x, fmaf(p.z, q.w, fmaf(-p.w, q.z, f[1]))));
         f[2] = fmaf(p.x, p.x, fmaf(p.y, p.y, fmaf(p.z, p.z, fmaf(p.w, p.w, f[2]))));
@@ -854,8 +857,12 @@ int ef_rowstats(const float* A, const float* B, int m, long long K, double* out,
     long long K2 = K / 2;
     long long kchunk = (K2 + nc - 1) / nc;
     ef_count_launches(1);
-    rowstats_kernel<<<dim3(nc, m), DTHREADS, 0, st>>>((const float4*)A, (const float4*)B, K2, kchunk,
-                                                     (double4*)work);
+    if (A == B)
+      rowstats_kernel<true><<<dim3(nc, m), DTHREADS, 0, st>>>((const float4*)A, (const float4*)B, K2,
+                                                             kchunk, (double4*)work);
+    else
+      rowstats_kernel<false><<<dim3(nc, m), DTHREADS, 0, st>>>((const float4*)A, (const float4*)B, K2,
+                                                              kchunk, (double4*)work);
   } else {
     long long kchunk = (K + nc - 1) / nc;
     ef_count_launches(1);

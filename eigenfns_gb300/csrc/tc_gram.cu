@@ -22,16 +22,18 @@
 // and added into fp32 registers while the next segment's MMAs run; a work unit's sum
 // goes out in fp64 and units (K-chunks, and the two K-ranges) are reduced in fp64.
 //
-// A persistent CTA (448 threads) walks work units (A-tile, B-tile, K-chunk):
-//   warp 13      loads: per 32-complex stage two 2-D TMA boxes (128-byte swizzle, zero
+// A persistent CTA (576 threads) walks work units (A-tile, B-tile, K-chunk):
+//   warp 17      loads: per 32-complex stage two 2-D TMA boxes (128-byte swizzle, zero
 //                fill outside) of the unit's A rows and two of its B rows into a raw
 //                shared-memory ring (the shared memory the operand ring leaves);
-//   warps 0-7    two groups of four converter warps, each taking every other stage:
+//   warps 0-11   three groups of four converter warps, taking the stages round robin
+//                (a group's wait-convert-store chain per stage is longer than a stage's
+//                share of HBM time, so three chains run staggered):
 //                A rows hi/lo split and tcgen05.st into a ring of TMEM operand stages
 //                (the MMA's A operand lives in TMEM, one A or A' row per lane), B rows
 //                hi/lo split into a ring of K-major shared-memory stages;
-//   warp 12      one thread issues each stage's MMAs and commits them;
-//   warps 8-11   drain finished segments (one TMEM lane per thread, all columns)
+//   warp 16      one thread issues each stage's MMAs and commits them;
+//   warps 12-15  drain finished segments (one TMEM lane per thread, all columns)
 //                and write the unit's partial sums.
 // Every mbarrier wait is bounded; on timeout the kernel sets the error flag, stops,
 // waits (bounded) for its own copies and MMAs and frees its TMEM.
@@ -55,10 +57,12 @@ namespace {
 
 using namespace ef::tc;
 
-constexpr int GC_THREADS = 448;
-constexpr int GC_GROUP = 128;         // converter threads per stage (warps 0-3 or 4-7)
-constexpr int GC_MMA_WARP = 12;
-constexpr int GC_LOAD_WARP = 13;
+constexpr int GC_NGROUPS = 3;         // converter groups, taking stages round robin
+constexpr int GC_GROUP = 128;         // converter threads per stage (one group of 4 warps)
+constexpr int GC_DRAIN_WARP = 4 * GC_NGROUPS;          // first of the 4 drain warps
+constexpr int GC_MMA_WARP = GC_DRAIN_WARP + 4;
+constexpr int GC_LOAD_WARP = GC_MMA_WARP + 1;
+constexpr int GC_THREADS = 32 * (GC_LOAD_WARP + 1);     // 576
 constexpr int GC_KB = 64;             // reals per stage (32 complex) = 8 k-steps of 8
 constexpr int GC_BOX = 32;            // reals per TMA box row (128 bytes, the swizzle width)
 constexpr int GC_RAW_MAX = 12;        // raw box stages at most (the rest of shared memory)
@@ -115,9 +119,9 @@ struct GcCfg {
   static constexpr int SEG = GC_SEG * PK;                      // stages per segment (32 k-steps)
 };
 
-// 14 warps: at most 4 per SM sub-partition, so 128 registers a thread fit
+// 18 warps: 576 threads x 112 registers fit the SM's 65,536
 template <int NB, int PK>
-__global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_constant__ CUtensorMap map_a,
+__global__ void __maxnreg__(112) tc_gram_kernel(const GcArgs a, const __grid_constant__ CUtensorMap map_a,
                                                 const __grid_constant__ CUtensorMap map_b) {
   using Cfg = GcCfg<NB, PK>;
   constexpr int GC_NBUF = Cfg::NBUF;
@@ -181,10 +185,10 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
     nst = kend > kbeg ? (int)((kend - kbeg + GC_KB / 2 - 1) / (GC_KB / 2)) : 0;
   };
 
-  if (warp < 8) {
+  if (warp < GC_DRAIN_WARP) {
     // ---------------- converters ----------------
-    // Two groups of four warps take alternate stages (group g the stages s with s % 2 == g),
-    // so one stage's waits and TMEM stores overlap the next stage's work. In a group,
+    // Three groups of four warps take the stages round robin (group g the stages s with
+    // s % 3 == g), so one stage's waits and TMEM stores overlap the next stages' work. In a group,
     // thread t (TMEM lane t) converts:
     //   A rows: lane l < mt is A row l, mt <= l < 2mt is A' row l - mt; PK = 1: l = t, both
     //   halves of the stage; PK = 2: l = t & 63, the half t >> 6 (reals [32 h, 32 h + 32));
@@ -207,7 +211,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
       long long kend = kbeg + a.kchunk;
       if (kend > a.K) kend = a.K;
       for (int st = 0; st < nst; ++st, ++s) {
-        if ((int)(s & 1) != grp) continue;
+        if ((int)(s % GC_NGROUPS) != grp) continue;
         const int slot = (int)(s % GC_RAW);
         const int o = (int)(s % nbuf);
         if (!mbar_wait(&raw_full[slot], (uint32_t)((s / GC_RAW) & 1)) ||
@@ -277,7 +281,7 @@ __global__ void __maxnreg__(128) tc_gram_kernel(const GcArgs a, const __grid_con
         mbar_arrive(&op_full[o]);
       }
     }
-  } else if (warp < 12) {
+  } else if (warp < GC_MMA_WARP) {
     // ---------------- drain ----------------
     const int lq = warp & 3;
     const int L = lq * 32 + lane;                       // TMEM lane = M row

@@ -116,7 +116,7 @@ class EigenServer:
     grouped solve; the running groups advance in one pipelined batch."""
 
     def __init__(self, budget_bytes: float = 160e9, max_concurrent: int = 16, device=None,
-                 group_wait: float = 0.3, min_group: int = 8, max_group: int = 32):
+                 group_wait: float = 0.5, min_group: int = 12, max_group: int = 32):
         self.budget = float(budget_bytes)
         self.max_concurrent = int(max_concurrent)
         self.group_wait = float(group_wait)

@@ -7,6 +7,7 @@
     python profile_kernels.py cheb --grid 192 --m 8 --steps 8
     python profile_kernels.py kpm --grid 256 --m 4 --steps 8
     python profile_kernels.py rowstats --ma 32 --mb 32 --grid 128
+    python profile_kernels.py rownorms --ma 64 --grid 128
 
 Each runs 3 warm-up calls and then --reps timed calls (default 1; CUDA events on
 the current stream), printing the mean time; under ncu, skip the warm-up launches
@@ -48,7 +49,7 @@ def _timed(fn, warm: int = 3) -> float:
 def main(argv=None) -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("kernel", choices=["theta", "precond", "gram", "gram_tc", "rotate", "cheb", "kpm",
-                                       "rowstats", "residual"])
+                                       "rowstats", "rownorms", "residual"])
     ap.add_argument("--grid", type=int, default=128)
     ap.add_argument("--m", type=int, default=2)
     ap.add_argument("--ma", type=int, default=32)
@@ -86,6 +87,8 @@ def main(argv=None) -> None:
         B = torch.randn((a.mb, K), dtype=torch.complex64, device="cuda", generator=g)
         if a.kernel == "rowstats":
             ms = _timed(lambda: blas.rowstats(A, B[: a.ma]))
+        elif a.kernel == "rownorms":                # rowstats of a block with itself
+            ms = _timed(lambda: blas.rowstats(A, A))
         elif a.kernel == "residual":
             lam = torch.rand(a.ma, dtype=torch.float64, device="cuda")
             R = torch.empty_like(A)
@@ -97,7 +100,10 @@ def main(argv=None) -> None:
         else:
             C = np.random.default_rng(2).standard_normal((a.ma, a.mb)).astype(np.complex64)
             ms = _timed(lambda: blas.rotate(C, A, B))
-        print(f"{a.kernel} {a.ma}x{a.mb} K={K}: {ms:.3f} ms")
+        rows = {"gram": a.ma + a.mb, "gram_tc": a.ma + a.mb, "rowstats": 2 * a.ma, "rownorms": a.ma,
+                "residual": 3 * a.ma}.get(a.kernel, a.ma + a.mb)
+        print(f"{a.kernel} {a.ma}x{a.mb} K={K}: {ms:.3f} ms  ({8.0 * K * rows / (ms * 1e-3) / 1e9:.0f} GB/s "
+              f"of {rows} rows read or written)")
 
 
 if __name__ == "__main__":
