@@ -62,7 +62,7 @@ constexpr int GC_GROUP = 128;         // converter threads per stage (one group 
 constexpr int GC_DRAIN_WARP = 4 * GC_NGROUPS;          // first of the 4 drain warps
 constexpr int GC_MMA_WARP = GC_DRAIN_WARP + 4;
 constexpr int GC_LOAD_WARP = GC_MMA_WARP + 1;
-constexpr int GC_THREADS = 32 * (GC_LOAD_WARP + 1);     // 576
+constexpr int GC_THREADS = 32 * (GC_LOAD_WARP + 1);     // 576 (18 warps)
 constexpr int GC_KB = 64;             // reals per stage (32 complex) = 8 k-steps of 8
 constexpr int GC_BOX = 32;            // reals per TMA box row (128 bytes, the swizzle width)
 constexpr int GC_RAW_MAX = 12;        // raw box stages at most (the rest of shared memory)
@@ -119,9 +119,10 @@ struct GcCfg {
   static constexpr int SEG = GC_SEG * PK;                      // stages per segment (32 k-steps)
 };
 
-// 18 warps: 576 threads x 112 registers fit the SM's 65,536
+// 18 warps, up to 5 on one SM sub-partition, whose 16,384 registers hold 5 warps x 32 x
+// 96 registers (15,360)
 template <int NB, int PK>
-__global__ void __maxnreg__(112) tc_gram_kernel(const GcArgs a, const __grid_constant__ CUtensorMap map_a,
+__global__ void __maxnreg__(96) tc_gram_kernel(const GcArgs a, const __grid_constant__ CUtensorMap map_a,
                                                 const __grid_constant__ CUtensorMap map_b) {
   using Cfg = GcCfg<NB, PK>;
   constexpr int GC_NBUF = Cfg::NBUF;
@@ -249,27 +250,30 @@ __global__ void __maxnreg__(112) tc_gram_kernel(const GcArgs a, const __grid_con
         }
         // A rows -> TMEM operand stage
         const uint32_t col = COL_A + (uint32_t)(o * Cfg::ACOLS);
+        // in quarters of 16 reals (4 quads), so that a converter thread holds 32 values
 #pragma unroll 1
-        for (int h2 = 0; h2 < 2 / PK; ++h2) {
+        for (int h4 = 0; h4 < 4 / PK; ++h4) {
+          const int h2 = h4 >> 1, qh = h4 & 1;
           const int hf = PK == 2 ? rg : h2;
-          float h[32], lo[32];
+          float h[16], lo[16];
 #pragma unroll
-          for (int q = 0; q < 8; ++q) {
+          for (int qq = 0; qq < 4; ++qq) {
+            const int q = 4 * qh + qq;
             float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
             if (aact && 2 * (8 * hf + q) < rem)
               x = *reinterpret_cast<const float4*>(rs + hf * MTMAX * 128 + ar * 128 + ((q ^ (ar & 7)) << 4));
             if (aprime) x = make_float4(-x.y, x.x, -x.w, x.z);   // (-ai, ar) per complex
-            h[4 * q] = x.x;
-            h[4 * q + 1] = x.y;
-            h[4 * q + 2] = x.z;
-            h[4 * q + 3] = x.w;
+            h[4 * qq] = x.x;
+            h[4 * qq + 1] = x.y;
+            h[4 * qq + 2] = x.z;
+            h[4 * qq + 3] = x.w;
           }
 #pragma unroll
-          for (int e = 0; e < 32; ++e) {
+          for (int e = 0; e < 16; ++e) {
             split_tf32(h[e], h[e], lo[e]);
           }
-          tmem_st32(lane_base + col + h2 * GC_BOX, h);
-          tmem_st32(lane_base + col + GC_KB / PK + h2 * GC_BOX, lo);
+          tmem_st16(lane_base + col + h2 * GC_BOX + 16 * qh, h);
+          tmem_st16(lane_base + col + GC_KB / PK + h2 * GC_BOX + 16 * qh, lo);
         }
         tmem_wait_st();
         fence_async_smem();
