@@ -28,7 +28,9 @@
 //                shared-memory ring (the shared memory the operand ring leaves);
 //   warps 0-11   three groups of four converter warps, taking the stages round robin
 //                (a group's wait-convert-store chain per stage is longer than a stage's
-//                share of HBM time, so three chains run staggered):
+//                share of HBM time, so three chains run staggered; two groups, 448
+//                threads and warps shifted down by 4, where the TMEM operand ring holds
+//                only two stages):
 //                A rows hi/lo split and tcgen05.st into a ring of TMEM operand stages
 //                (the MMA's A operand lives in TMEM, one A or A' row per lane), B rows
 //                hi/lo split into a ring of K-major shared-memory stages;
@@ -57,12 +59,7 @@ namespace {
 
 using namespace ef::tc;
 
-constexpr int GC_NGROUPS = 3;         // converter groups, taking stages round robin
 constexpr int GC_GROUP = 128;         // converter threads per stage (one group of 4 warps)
-constexpr int GC_DRAIN_WARP = 4 * GC_NGROUPS;          // first of the 4 drain warps
-constexpr int GC_MMA_WARP = GC_DRAIN_WARP + 4;
-constexpr int GC_LOAD_WARP = GC_MMA_WARP + 1;
-constexpr int GC_THREADS = 32 * (GC_LOAD_WARP + 1);     // 576 (18 warps)
 constexpr int GC_KB = 64;             // reals per stage (32 complex) = 8 k-steps of 8
 constexpr int GC_BOX = 32;            // reals per TMA box row (128 bytes, the swizzle width)
 constexpr int GC_RAW_MAX = 12;        // raw box stages at most (the rest of shared memory)
@@ -117,10 +114,35 @@ struct GcCfg {
                                   : GC_RAW_MAX;
   static_assert(NBUF >= 2 && NRAW >= 4, "operand and raw rings");
   static constexpr int SEG = GC_SEG * PK;                      // stages per segment (32 k-steps)
+  // converter groups, taking the stages round robin. A group's wait for an operand
+  // buffer is by phase parity, which is only unambiguous while the buffer's previous
+  // user, NBUF stages back, is a stage the waiting group has already seen retire; with
+  // NG groups a group's previous stage is NG back, so NG <= NBUF.
+  static constexpr int NG = NBUF >= 3 ? 3 : 2;
+  static constexpr int DRAIN_WARP = 4 * NG;                    // first of the 4 drain warps
+  static constexpr int MMA_WARP = DRAIN_WARP + 4;
+  static constexpr int LOAD_WARP = MMA_WARP + 1;
+  static constexpr int THREADS = 32 * (LOAD_WARP + 1);         // 576 (NG = 3) or 448
+  // raw slots are owned by groups: stage s goes to slot (s % NG) + NG * ((s / NG) % RPG),
+  // so a slot's consecutive stages belong to one group, which has consumed the slot's
+  // previous phase before it waits on the next (no parity aliasing between groups)
+  static constexpr int RPG = NRAW / NG;                        // raw slots per group
+  static constexpr int NRAW_USED = RPG * NG;
+  static_assert(RPG >= 1, "a raw slot per converter group");
 };
 
-// 18 warps, up to 5 on one SM sub-partition, whose 16,384 registers hold 5 warps x 32 x
-// 96 registers (15,360)
+// raw slot of stage s and how many earlier stages used that slot
+template <int NG, int RPG>
+__device__ __forceinline__ int raw_slot(uint32_t s) {
+  return (int)(s % NG) + NG * (int)((s / NG) % RPG);
+}
+template <int NG, int RPG>
+__device__ __forceinline__ uint32_t raw_use(uint32_t s) {
+  return (s / NG) / RPG;
+}
+
+// up to 18 warps, up to 5 on one SM sub-partition, whose 16,384 registers hold 5 warps x
+// 32 x 96 registers (15,360)
 template <int NB, int PK>
 __global__ void __maxnreg__(96) tc_gram_kernel(const GcArgs a, const __grid_constant__ CUtensorMap map_a,
                                                 const __grid_constant__ CUtensorMap map_b) {
@@ -166,6 +188,7 @@ __global__ void __maxnreg__(96) tc_gram_kernel(const GcArgs a, const __grid_cons
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  constexpr int GC_MMA_WARP = Cfg::MMA_WARP, GC_LOAD_WARP = Cfg::LOAD_WARP, GC_NGROUPS = Cfg::NG;
   if (warp == GC_MMA_WARP) tmem_alloc(&tmem_base_s, TCOLS);
   fence_before_sync();
   __syncthreads();
@@ -186,7 +209,7 @@ __global__ void __maxnreg__(96) tc_gram_kernel(const GcArgs a, const __grid_cons
     nst = kend > kbeg ? (int)((kend - kbeg + GC_KB / 2 - 1) / (GC_KB / 2)) : 0;
   };
 
-  if (warp < GC_DRAIN_WARP) {
+  if (warp < Cfg::DRAIN_WARP) {
     // ---------------- converters ----------------
     // Three groups of four warps take the stages round robin (group g the stages s with
     // s % 3 == g), so one stage's waits and TMEM stores overlap the next stages' work. In a group,
@@ -213,9 +236,9 @@ __global__ void __maxnreg__(96) tc_gram_kernel(const GcArgs a, const __grid_cons
       if (kend > a.K) kend = a.K;
       for (int st = 0; st < nst; ++st, ++s) {
         if ((int)(s % GC_NGROUPS) != grp) continue;
-        const int slot = (int)(s % GC_RAW);
+        const int slot = raw_slot<Cfg::NG, Cfg::RPG>(s);
         const int o = (int)(s % nbuf);
-        if (!mbar_wait(&raw_full[slot], (uint32_t)((s / GC_RAW) & 1)) ||
+        if (!mbar_wait(&raw_full[slot], raw_use<Cfg::NG, Cfg::RPG>(s) & 1u) ||
             !mbar_wait(&op_empty[o], (uint32_t)(((s / nbuf) + 1) & 1))) {
           abort_s = 1;
           atomicExch(a.err, 1);
@@ -397,8 +420,8 @@ __global__ void __maxnreg__(96) tc_gram_kernel(const GcArgs a, const __grid_cons
       unit_of(k, it, jt, kc, kbeg, nst);
       const int i0 = it * a.mt, j0 = jt * NB;
       for (int st = 0; st < nst; ++st, ++s) {
-        const int slot = (int)(s % GC_RAW);
-        if (!mbar_wait(&raw_empty[slot], (uint32_t)(((s / GC_RAW) + 1) & 1), 64u)) {
+        const int slot = raw_slot<Cfg::NG, Cfg::RPG>(s);
+        if (!mbar_wait(&raw_empty[slot], (raw_use<Cfg::NG, Cfg::RPG>(s) + 1u) & 1u, 64u)) {
           abort_s = 1;
           atomicExch(a.err, 1);
           break;
@@ -415,8 +438,8 @@ __global__ void __maxnreg__(96) tc_gram_kernel(const GcArgs a, const __grid_cons
       }
     }
     // no copy may still be landing when the CTA exits: wait for the last issued phases
-    for (uint32_t t = issued > (uint32_t)GC_RAW ? issued - GC_RAW : 0; t < issued; ++t)
-      mbar_wait(&raw_full[(int)(t % GC_RAW)], (uint32_t)((t / GC_RAW) & 1));
+    for (uint32_t t = issued > (uint32_t)Cfg::NRAW_USED ? issued - Cfg::NRAW_USED : 0; t < issued; ++t)
+      mbar_wait(&raw_full[raw_slot<Cfg::NG, Cfg::RPG>(t)], raw_use<Cfg::NG, Cfg::RPG>(t) & 1u);
   }
   fence_before_sync();
   __syncthreads();
@@ -539,7 +562,7 @@ int launch_gc(const GcPlan& p, cudaStream_t st, const float* A, const float* B, 
   long long units = (long long)p.nit * p.njt * p.nk;
   long long grid = sm_count_dev();
   if (grid > units) grid = units;
-  tc_gram_kernel<NB, PK><<<(unsigned)grid, GC_THREADS, smem, st>>>(a, ma_map, mb_map);
+  tc_gram_kernel<NB, PK><<<(unsigned)grid, GcCfg<NB, PK>::THREADS, smem, st>>>(a, ma_map, mb_map);
   return EF_OK;
 }
 
