@@ -28,7 +28,7 @@ import torch
 
 from . import blas, hosteig
 from .grouped import GroupResults
-from .solver import HostEigh, lobpcg_steps
+from .solver import HostEigh, HostMany, lobpcg_steps
 
 
 class _EighOnHost:
@@ -46,6 +46,8 @@ def _pinned_copy(t: torch.Tensor) -> torch.Tensor:
 
 def _request_to_host(req):
     """Queue the copy of a request's device tensors to pinned host memory."""
+    if isinstance(req, HostMany):
+        return [_request_to_host(r) for r in req.items]
     if isinstance(req, HostEigh):
         return _EighOnHost(_pinned_copy(req.A))
     if isinstance(req, tuple):
@@ -55,6 +57,8 @@ def _request_to_host(req):
 
 def _host_data(h):
     """What the solve is sent back: numpy copies, or the fp64 eigh it asked for."""
+    if isinstance(h, list):
+        return [_host_data(x) for x in h]
     if isinstance(h, _EighOnHost):
         A = h.A.numpy()
         return hosteig.eigh_many(A) if A.ndim == 3 else hosteig.eigh(A)

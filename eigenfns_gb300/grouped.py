@@ -29,7 +29,8 @@ import torch
 
 from . import blas, dense
 from ._lib import EF_RAND_NORMAL, call, load
-from .solver import _RR_DEAD_PENALTY, _SVQB_DROP, HostEigh, SolveStats, svqb_from_eig
+from .solver import (_RR_DEAD_PENALTY, _SVQB_DROP, HostEigh, HostMany, SolveStats, _ritz_from_host,
+                     svqb_from_eig)
 
 
 class GroupResults:
@@ -181,9 +182,15 @@ def lobpcg_group_steps(ops, nevs, keys=None, m: int = 32, guard: int = 8, tol: f
         scale = 1.0 / torch.clamp(torch.sqrt(torch.clamp(sq[:, :, 2], min=0.0)), min=floor)
         st.scale_rows(idx, Xv, scale, rows)
 
-    def ortho_steps(idx, Xv):
-        """SVQB pass on host eigh, then the device Cholesky-QR pass (solver._ortho_steps)."""
+    def ortho_steps(idx, Xv, first=None):
+        """SVQB pass on host eigh, then the device Cholesky-QR pass (solver._ortho_steps);
+        `first` is the host eigh of the first pass's Gram when the caller has read it."""
         for p in range(2):
+            if p == 0 and first is not None:
+                w, V = first
+                C = np.stack([svqb_from_eig(w[j], V[j], _SVQB_DROP)[0] for j in range(len(idx))])
+                rotate_inplace(idx, st.upload(idx, C.astype(np.complex64), (m, m)), Xv, m)
+                continue
             Gm = st.gram(idx, Xv, Xv, m, m)
             if p > 0 and m <= dense.MAX_N:
                 C, _ = dense.cholqr_coeffs(Gm[idx_t(idx)], tol=_SVQB_DROP)
@@ -214,16 +221,18 @@ def lobpcg_group_steps(ops, nevs, keys=None, m: int = 32, guard: int = 8, tol: f
             idx_cache[key] = t
         return t
 
-    def ritz(idx, Xv, HXv, Wv, normalize):
-        """(lam, rn, |x|) per member of idx, R = HX - lam X into W (solver._ritz_steps)."""
+    def ritz_request(idx, Xv, HXv, Wv, normalize):
+        """Queue (lam, |x|^2, |Θx|^2, |R|^2) per row of the members idx, with R = HX -
+        lam X into W (solver._ritz_request); (len(idx), m, 4) on the device."""
         s = st.rowstats(idx, Xv, HXv, m)
         lam_d = s[:, :, 0] / torch.clamp(s[:, :, 2], min=1e-30) if normalize else s[:, :, 0].contiguous()
         r2 = st.residual_norms(idx, HXv, Xv, lam_d, Wv, m)
         sel = idx_t(idx)
-        h = yield torch.stack([lam_d[sel], s[sel][:, :, 2], s[sel][:, :, 3], r2[sel]], dim=2)
-        lam, xx, hh, rr = h[:, :, 0], h[:, :, 1], h[:, :, 2], h[:, :, 3]
-        rn = np.sqrt(np.maximum(rr, 0.0)) / np.maximum(np.sqrt(np.maximum(hh, 0.0)), 1e-30)
-        return lam, rn, np.sqrt(np.maximum(xx, 0.0))
+        return torch.stack([lam_d[sel], s[sel][:, :, 2], s[sel][:, :, 3], r2[sel]], dim=2)
+
+    def ritz(idx, Xv, HXv, Wv, normalize):
+        """(lam, rn, |x|) per member of idx (solver._ritz_steps)."""
+        return _ritz_from_host((yield ritz_request(idx, Xv, HXv, Wv, normalize)))
 
     def rr_gram(idx, act, hact, nb):
         """Block upper triangle of act^H (Θ act) and its conjugate (solver._rr_gram)."""
@@ -264,8 +273,18 @@ def lobpcg_group_steps(ops, nevs, keys=None, m: int = 32, guard: int = 8, tol: f
             c = 0 if it % 2 == 0 else 1            # active members flip slabs together
             P, X, W = blocks(c)
             S = slabs[c]
-            lam, rn, xnorm = yield from ritz(active, X, HX, W, False)
-            still = []
+            # the work up to W's first SVQB Gram touches W only: queued before the
+            # convergence test, read with it (solver.lobpcg_steps does the same)
+            ritz_t = ritz_request(active, X, HX, W, False)
+            st.theta(active, W, W, m, precondition=True)
+            deflate(active, W)
+            for _ in range(2):
+                Cm = st.gram(active, X, W, m, m).to(torch.complex64)
+                st.rotate(active, Cm, X, W, m, m, -1)
+            Gw = st.gram(active, W, W, m, m)
+            h, (ww, Vw) = yield HostMany([ritz_t, HostEigh(_hermitian(Gw[idx_t(active)]))])
+            lam, rn, xnorm = _ritz_from_host(h)
+            still, keep = [], []
             for j, i in enumerate(active):
                 dead = xnorm[j] < 0.5
                 lam_h = np.where(dead, np.inf, lam[j])
@@ -276,16 +295,12 @@ def lobpcg_group_steps(ops, nevs, keys=None, m: int = 32, guard: int = 8, tol: f
                     cur[i] = c
                 else:
                     still.append(i)
+                    keep.append(j)
                     stats[i].iterations += 1
             active = still
             if not active:
                 break
-            st.theta(active, W, W, m, precondition=True)
-            deflate(active, W)
-            for _ in range(2):
-                Cm = st.gram(active, X, W, m, m).to(torch.complex64)
-                st.rotate(active, Cm, X, W, m, m, -1)
-            yield from ortho_steps(active, W)
+            yield from ortho_steps(active, W, first=(ww[keep], Vw[keep]))
             with_p = [i for i in active if have_p[i]]
             if with_p:
                 XW = S[:, m:3 * m]

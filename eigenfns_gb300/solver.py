@@ -70,6 +70,15 @@ class HostEigh:
         self.A = A
 
 
+class HostMany:
+    """A step generator's request for several host reads at once: a list of device
+    tensors and HostEigh requests; the driver sends back the list of their results."""
+    __slots__ = ("items",)
+
+    def __init__(self, items):
+        self.items = list(items)
+
+
 def _hermitian(G: torch.Tensor) -> torch.Tensor:
     return 0.5 * (G + G.conj().T)
 
@@ -112,9 +121,10 @@ def _theta(op, X, stats, out=None):
     return op.theta(X, out=out)
 
 
-def _ortho_steps(X: torch.Tensor, passes: int = 2, drop: float = _SVQB_DROP):
+def _ortho_steps(X: torch.Tensor, passes: int = 2, drop: float = _SVQB_DROP, first=None):
     """SVQB on a contiguous block slot, written back into the slot (a step generator:
-    it yields the one device matrix it reads on the host).
+    it yields the one device matrix it reads on the host; `first`, the host eigh of the
+    symmetrised Gram X^H X already read by the caller, replaces that read).
 
     The first pass is the reference's SVQB (host fp64 eigh with the 1e-5 drop). After it
     every row is unit or zero, so the second pass is a well-conditioned re-orthonormalisation
@@ -127,7 +137,10 @@ def _ortho_steps(X: torch.Tensor, passes: int = 2, drop: float = _SVQB_DROP):
         if p > 0 and m <= dense.MAX_N:
             C, _ = dense.cholqr_coeffs(gram(X, X), tol=drop)
         else:
-            w, V = yield HostEigh(_hermitian(gram(X, X)))
+            if p == 0 and first is not None:
+                w, V = first
+            else:
+                w, V = yield HostEigh(_hermitian(gram(X, X)))
             C, _ = svqb_from_eig(w, V, drop)
             C = C.astype(np.complex64)
         if m <= 32:
@@ -141,6 +154,8 @@ def _ortho_inplace(X: torch.Tensor, passes: int = 2, drop: float = _SVQB_DROP) -
 
 
 def _to_host(req):
+    if isinstance(req, HostMany):
+        return [_to_host(r) for r in req.items]
     if isinstance(req, HostEigh):
         from . import hosteig
         A = req.A.cpu().numpy()
@@ -186,18 +201,26 @@ def _rr_gram(act: torch.Tensor, hact: torch.Tensor, m: int) -> torch.Tensor:
     return A
 
 
-def _ritz_steps(X, HX, R, normalize: bool):
-    """(lam, relres, |x|) for the rows of X, with R = HX - lam X written into `R`.
-
-    One pass for <x, Θx>, |x|^2, |Θx|^2 and one fused pass that forms R and |R|^2;
-    the small per-row vectors reach the host in a single copy (the one yield)."""
+def _ritz_request(X, HX, R, normalize: bool) -> torch.Tensor:
+    """Queue the per-row (lam, |x|^2, |Θx|^2, |R|^2) of X, with R = HX - lam X written
+    into `R`: one pass for <x, Θx>, |x|^2, |Θx|^2 and one fused pass for R and |R|^2."""
     st = blas.rowstats(X, HX)
     lam_d = st[:, 0] / torch.clamp(st[:, 2], min=1e-30) if normalize else st[:, 0].contiguous()
     r2 = blas.residual_norms(HX, X, lam_d, R)
-    h = yield torch.cat([lam_d[:, None], st[:, 2:4], r2[:, None]], dim=1)
-    lam, xx, hh, rr = h[:, 0], h[:, 1], h[:, 2], h[:, 3]
+    return torch.cat([lam_d[:, None], st[:, 2:4], r2[:, None]], dim=1)
+
+
+def _ritz_from_host(h):
+    """(lam, relres, |x|) from the host copy of a _ritz_request."""
+    lam, xx, hh, rr = h[..., 0], h[..., 1], h[..., 2], h[..., 3]
     rn = np.sqrt(np.maximum(rr, 0.0)) / np.maximum(np.sqrt(np.maximum(hh, 0.0)), 1e-30)
     return lam, rn, np.sqrt(np.maximum(xx, 0.0))
+
+
+def _ritz_steps(X, HX, R, normalize: bool):
+    """(lam, relres, |x|) for the rows of X, with R = HX - lam X written into `R`; the
+    small per-row vectors reach the host in a single copy (the one yield)."""
+    return _ritz_from_host((yield _ritz_request(X, HX, R, normalize)))
 
 
 def lobpcg_steps(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
@@ -270,8 +293,17 @@ def lobpcg_steps(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
         n_lock = min(m - guard, nev - locked_vals.size)
         it = 0
         for it in range(maxit):
-            # R = HX - lam X lands in the W slot, where the preconditioner needs it
-            lam, rn, xnorm = yield from _ritz_steps(X, HX, W, False)
+            # R = HX - lam X lands in the W slot, where the preconditioner needs it. The
+            # iteration's work up to the first SVQB Gram of W touches W only, so it is
+            # queued before the convergence test and both reach the host in one read (if
+            # the block has converged, W is recomputed at the block's end).
+            ritz = _ritz_request(X, HX, W, False)
+            op.precondition(W, out=W)
+            deflate(W, locked, deflate_chunk)
+            for _ in range(2):
+                rotate(gram(X, W).to(torch.complex64), X, W, -1)
+            h, eig_w = yield HostMany([ritz, HostEigh(_hermitian(gram(W, W)))])
+            lam, rn, xnorm = _ritz_from_host(h)
             dead_rows = xnorm < 0.5
             lam_h = np.where(dead_rows, np.inf, lam)
             rn = np.where(dead_rows, np.inf, rn)
@@ -284,11 +316,7 @@ def lobpcg_steps(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
                       f"{lo[-1]:.4f}  res q50/q90 {np.quantile(rn, 0.5):.1e}/{np.quantile(rn, 0.9):.1e}",
                       flush=True)
             stats.iterations += 1
-            op.precondition(W, out=W)
-            deflate(W, locked, deflate_chunk)
-            for _ in range(2):
-                rotate(gram(X, W).to(torch.complex64), X, W, -1)
-            yield from _ortho_steps(W)
+            yield from _ortho_steps(W, first=eig_w)
             if have_p:
                 XW = S[m:3 * m]
                 for _ in range(2):
