@@ -143,9 +143,12 @@ def gram_tc(A: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
 
 
 def _coef(C, device) -> torch.Tensor:
+    """Coefficients on the device as complex64. A host array goes through pinned staging
+    and an asynchronous copy, so the host does not wait for the work queued before it."""
     if isinstance(C, torch.Tensor):
         return C.to(device=device, dtype=torch.complex64).contiguous()
-    return torch.from_numpy(np.ascontiguousarray(np.asarray(C, np.complex64))).to(device)
+    h = torch.from_numpy(np.ascontiguousarray(np.asarray(C, np.complex64)))
+    return h.pin_memory().to(device, non_blocking=True)
 
 
 def rotate(C, S: torch.Tensor, out: torch.Tensor | None = None, mode: int = 0) -> torch.Tensor:

@@ -124,6 +124,11 @@ class _Stack:
         return pinned.to(self.device, non_blocking=True)
 
 
+def _to_device(a: np.ndarray, dev) -> torch.Tensor:
+    """A small host array on the device without waiting for the stream (pinned staging)."""
+    return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().to(dev, non_blocking=True)
+
+
 def _hermitian(A: torch.Tensor) -> torch.Tensor:
     return 0.5 * (A + A.conj().transpose(-2, -1))
 
@@ -217,7 +222,7 @@ def lobpcg_group_steps(ops, nevs, keys=None, m: int = 32, guard: int = 8, tol: f
         key = tuple(int(i) for i in idx)
         t = idx_cache.get(key)
         if t is None:
-            t = torch.tensor(key, dtype=torch.long, device=dev)
+            t = _to_device(np.asarray(key, dtype=np.int64), dev)
             idx_cache[key] = t
         return t
 
@@ -385,8 +390,8 @@ def lobpcg_group_steps(ops, nevs, keys=None, m: int = 32, guard: int = 8, tol: f
                     f"pairs but needs {k} to lock — rank collapse")
                 continue
             Xc = slabs[c][i, m:2 * m]
-            lock_idx = torch.from_numpy(np.asarray(order[:k])).to(dev)
-            carry_idx = torch.from_numpy(np.asarray(order[k:])).to(dev)
+            lock_idx = _to_device(np.asarray(order[:k], dtype=np.int64), dev)
+            carry_idx = _to_device(np.asarray(order[k:], dtype=np.int64), dev)
             locked_buf[i, n_locked:n_locked + k] = Xc.index_select(0, lock_idx)
             carry[i] = Xc.index_select(0, carry_idx)
             locked_vals[i] = np.concatenate([locked_vals[i], lam_j[order[:k]]])
@@ -397,7 +402,7 @@ def lobpcg_group_steps(ops, nevs, keys=None, m: int = 32, guard: int = 8, tol: f
                 vals = locked_vals[i]
                 order_v = np.argsort(vals, kind="stable")
                 n_i = vals.size
-                vecs = locked_buf[i, :n_i].index_select(0, torch.from_numpy(order_v).to(dev))
+                vecs = locked_buf[i, :n_i].index_select(0, _to_device(order_v.astype(np.int64), dev))
                 done[keys[i]] = (vals[order_v][:nevs[i]], vecs, stats[i])
                 carry[i] = None
             else:

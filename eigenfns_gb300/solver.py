@@ -367,8 +367,8 @@ def lobpcg_steps(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
             raise RuntimeError(
                 f"block produced only {int(np.isfinite(lam).sum())} live Ritz "
                 f"pairs but needs {n_lock} to lock — rank collapse")
-        lock_idx = torch.from_numpy(np.asarray(order[:n_lock])).to(dev)
-        carry_idx = torch.from_numpy(np.asarray(order[n_lock:])).to(dev)
+        lock_idx = torch.from_numpy(np.asarray(order[:n_lock])).pin_memory().to(dev, non_blocking=True)
+        carry_idx = torch.from_numpy(np.asarray(order[n_lock:])).pin_memory().to(dev, non_blocking=True)
         Xl = X.index_select(0, lock_idx)
         carry = X.index_select(0, carry_idx)
         locked_buf[n_locked_now:n_locked_now + n_lock] = Xl
