@@ -652,7 +652,8 @@ __global__ void mask_kernel(const float* kax, int G, float2* X, long long total)
 
 int grid_for(long long total) {
   long long b = (total + 255) / 256;
-  if (b > 152 * 16) b = 152 * 16;
+  const long long cap = 16LL * ef::sm_count();     // two waves of 8 resident 256-thread CTAs
+  if (b > cap) b = cap;
   if (b < 1) b = 1;
   return (int)b;
 }
@@ -829,7 +830,7 @@ int ef_rotate(const float* C, const float* S, float* out, int m_in, int m_out, l
   size_t smem = (size_t)m_in * RT * sizeof(float2);
   set_smem_once(rotate_kernel, smem);
   long long bx = (K + RTHREADS - 1) / RTHREADS;
-  long long cap = (152 * 8 + ty - 1) / ty;
+  long long cap = (8LL * ef::sm_count() + ty - 1) / ty;
   if (bx > cap) bx = cap;
   ef_count_launches(1);
   rotate_kernel<<<dim3((unsigned)bx, ty), RTHREADS, smem, st>>>((const float2*)C, (const float2*)S,

@@ -18,6 +18,22 @@ std::atomic<unsigned long long> g_launches{0};
 
 void ef_count_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
 
+namespace ef {
+int sm_count() {
+  static std::atomic<int> cached[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  int n = cached[dev].load(std::memory_order_relaxed);
+  if (n == 0) {
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+    cached[dev].store(n, std::memory_order_relaxed);
+  }
+  return n;
+}
+}  // namespace ef
+
 namespace {
 struct SmemEntry {
   const void* kernel;

@@ -80,6 +80,9 @@ __device__ __forceinline__ Frame frame_at(const float* __restrict__ kax,
 // and the pipeline launches its kernels hundreds of times per solve.
 void set_smem_limit(const void* kernel, size_t smem);
 
+// number of SMs of the current device (queried once per device)
+int sm_count();
+
 template <class K>
 inline void set_smem_once(K kernel, size_t smem) {
   if (smem > 48 * 1024) set_smem_limit(reinterpret_cast<const void*>(kernel), smem);

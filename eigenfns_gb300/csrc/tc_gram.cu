@@ -481,19 +481,6 @@ size_t gc_smem() {
   return s < (size_t)GC_SMEM_MIN ? (size_t)GC_SMEM_MIN : s;
 }
 
-int sm_count_dev() {
-  static int cached[64] = {0};
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev < 0 || dev >= 64) dev = 0;
-  if (cached[dev] == 0) {
-    int n = 0;
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    cached[dev] = n > 0 ? n : 1;
-  }
-  return cached[dev];
-}
-
 struct GcPlan {
   int mt, nb, pk, nit, njt, nk;
   long long kchunk;
@@ -526,7 +513,7 @@ GcPlan gc_plan(int ma, int mb, long long K, int units) {
   p.nit = (ma + p.mt - 1) / p.mt;
   p.njt = (mb + p.nb - 1) / p.nb;
   const long long tiles = (long long)p.nit * p.njt;
-  const long long sms = sm_count_dev();
+  const long long sms = ef::sm_count();
   long long nk = (units * sms + tiles - 1) / tiles;           // about `units` units per SM
   const long long maxk = (K + 2047) / 2048;                   // >= 2048 complex per unit
   if (nk > maxk) nk = maxk;
@@ -560,7 +547,7 @@ int launch_gc(const GcPlan& p, cudaStream_t st, const float* A, const float* B, 
   const size_t smem = gc_smem<NB, PK>();
   ef::set_smem_once(tc_gram_kernel<NB, PK>, smem);
   long long units = (long long)p.nit * p.njt * p.nk;
-  long long grid = sm_count_dev();
+  long long grid = ef::sm_count();
   if (grid > units) grid = units;
   tc_gram_kernel<NB, PK><<<(unsigned)grid, GcCfg<NB, PK>::THREADS, smem, st>>>(a, ma_map, mb_map);
   return EF_OK;

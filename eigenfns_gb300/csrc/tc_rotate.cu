@@ -299,19 +299,6 @@ __global__ void __maxnreg__(128) tc_rotate_kernel(const TrArgs a, const __grid_c
   if (warp == TR_MMA_WARP) tmem_dealloc(tmem, tcols);
 }
 
-int sm_count() {
-  static int cached[64] = {0};
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev < 0 || dev >= 64) dev = 0;
-  if (cached[dev] == 0) {
-    int n = 0;
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    cached[dev] = n > 0 ? n : 1;
-  }
-  return cached[dev];
-}
-
 size_t tr_smem(int nch, int mp) {
   const size_t s = (size_t)TR_RAW * TR_RAW_BYTES + (size_t)2 * (2 * mp) * (nch * TR_JC) * 4 + 1024;
   return s < (size_t)TR_SMEM_MIN ? (size_t)TR_SMEM_MIN : s;
@@ -359,7 +346,7 @@ int tc_rotate_launch(const float* C, int ldc, const float* S, float* out, int m_
     return ef_fail(EF_ERR_CUDA, "rotate: tensor map encoding failed");
   const size_t smem = tr_smem(a.nch, a.mp);
   ef::set_smem_once(tc_rotate_kernel, smem);
-  long long grid = sm_count();
+  long long grid = ef::sm_count();
   if (grid > a.ntiles) grid = a.ntiles;
   ef_count_launches(1);
   tc_rotate_kernel<<<(unsigned)grid, TR_THREADS, smem, st>>>(a, ms, mo);

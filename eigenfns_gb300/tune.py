@@ -2,8 +2,8 @@
 
 What it chooses
   operator  per (grid edge G, block size m): the three-pass pipeline (z / xy-plane / z,
-            for the grid edges that have a plan) with a sub-batch workspace of 1, 2 or 4
-            vectors, or the five-pass pencil pipeline; applied with
+            for the grid edges that have a plan) with a sub-batch workspace of 1, 2, 4, 8
+            or 16 vectors, or the five-pass pencil pipeline; applied with
             MaxwellOperator.configure (ef_op_configure).
   Gram      per (ma, mb) at a vector length K: the tensor-core kernel with 1, 2, 3 or 4
             K-chunks per SM, or the CUDA-core split-K kernel; registered with
@@ -78,7 +78,7 @@ def operator_candidates(op) -> list:
     out = [(5, 0)]
     try:
         op.configure(3, 0)
-        out = [(3, k * per_vec + 1) for k in (1, 2, 4)] + out
+        out = [(3, k * per_vec + 1) for k in (1, 2, 4, 8, 16)] + out
     except ValueError:
         pass                      # no three-pass plan for this grid edge
     finally:
