@@ -117,3 +117,26 @@ def test_group_by_shape_keeps_order_and_caps_size():
     ms = [16, 32, 16, 16, 32, 8]
     groups = group_by_shape(ops, ms, [4] * 6, max_group=2)
     assert groups == [[0, 2], [3], [1, 4], [5]]
+
+
+def test_combined_host_reads_and_stacked_eigh():
+    """A HostMany request comes back as the list of its parts' results: numpy copies for
+    tensors and (w, V) for HostEigh, stacked for a stack of matrices (one LAPACK call per
+    problem, the same numbers as for the matrix alone)."""
+    import numpy as np
+    from eigenfns_gb300.solver import HostEigh, HostMany, run_steps
+
+    rng = np.random.default_rng(3)
+    A = rng.standard_normal((3, 50, 50)) + 1j * rng.standard_normal((3, 50, 50))
+    A = A + A.conj().transpose(0, 2, 1)
+
+    def gen():
+        t, (w, V) = yield HostMany([torch.arange(4.0), HostEigh(torch.from_numpy(A))])
+        w1, V1 = yield HostEigh(torch.from_numpy(A[1]))
+        return t, w, V, w1, V1
+
+    t, w, V, w1, V1 = run_steps(gen())
+    assert np.array_equal(t, np.arange(4.0)) and w.shape == (3, 50) and V.shape == (3, 50, 50)
+    assert np.array_equal(w[1], w1) and np.array_equal(V[1], V1)
+    for i in range(3):
+        assert np.allclose(A[i] @ V[i], V[i] * w[i][None, :], atol=1e-10)
