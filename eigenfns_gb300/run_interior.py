@@ -45,10 +45,11 @@ def two_stage(op, lam_lo: float, lam_hi: float, m: int, lam_max: float = 0.0,
         lam_max = float(resume_state["lam_max"])
         history = list(resume_state.get("history", []))
 
-    def one_stage(X, stage_name, degree, first_outer, max_outers):
+    def one_stage(X, stage_name, degree, first_outer, max_outers, lam=None, rn=None):
+        """Outers of one stage; (lam, rn) are the previous stage's Ritz values, returned
+        as they are when the stage runs no outer."""
         nonlocal n_theta
         coef = bandpass_coeffs(lam_lo, lam_hi, lam_max, degree)
-        lam = rn = None
         for outer in range(first_outer, max_outers):
             t0 = time.perf_counter()
             if X is None:
@@ -85,11 +86,13 @@ def two_stage(op, lam_lo: float, lam_hi: float, m: int, lam_max: float = 0.0,
                 break
         return X, lam, rn
 
-    X = X0
+    X, lam, rn = X0, None, None
     if stage == "build":
         X, lam, rn = one_stage(X, "build", build_degree, outer0, build_outers)
         outer0 = 0
-    X, lam, rn = one_stage(X, "polish", polish_degree, outer0, polish_outers)
+    X, lam, rn = one_stage(X, "polish", polish_degree, outer0, polish_outers, lam, rn)
+    if lam is None:
+        raise ValueError("two_stage ran no outer: give build_outers or polish_outers > 0")
     inwin = np.isfinite(lam) & (lam >= lam_lo) & (lam <= lam_hi)
     conv = inwin & (rn < tol)
     unconv = inwin & ~conv

@@ -157,6 +157,12 @@ def test_two_stage_matches_reference(golden, gpu):
                     theta_chunk=int(tchunk), X_init=golden["two_X0"])
     assert res["vals"].shape == golden["two_vals"].shape
     assert np.allclose(res["vals"], golden["two_vals"], rtol=1e-5)
+    # build stage alone (no polish outer): the build's last Ritz values come back
+    b = two_stage(op, lo, hi, int(m), lam_max=lmax, build_degree=int(bd), build_outers=int(bo),
+                  polish_degree=int(pd), polish_outers=0, tol=tol, chunk=int(chunk),
+                  theta_chunk=int(tchunk), X_init=golden["two_X0"])
+    assert b["lam"].shape == (int(m),)
+    assert [h["stage"] for h in b["history"]] == ["build"] * int(bo)
 
 
 def test_rasterizer_matches_oracle(gpu):
