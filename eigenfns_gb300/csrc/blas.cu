@@ -226,7 +226,7 @@ __global__ void gram_reduce_kernel(const double2* __restrict__ partial, int nspl
 int gram_splits(int ma, int mb, long long K) {
   long long tiles = (long long)((ma + GT - 1) / GT) * ((mb + GT - 1) / GT);
   long long target = 4096 / (tiles > 0 ? tiles : 1);
-  long long maxs = (K + 2047) / 2048;   // at least 2048 k-values per chunk
+  long long maxs = (K + 255) / 256;     // at least 256 k-values per chunk (small K: more CTAs)
   long long s = target < maxs ? target : maxs;
   if (s < 1) s = 1;
   return (int)s;

@@ -65,6 +65,7 @@ constexpr int GC_BOX = 32;            // reals per TMA box row (128 bytes, the s
 constexpr int GC_RAW_MAX = 12;        // raw box stages at most (the rest of shared memory)
 constexpr int GC_SEG = 4;             // stages per TMEM accumulation segment (32 k-steps)
 constexpr int GC_SMEM_MIN = 120 * 1024;   // keeps one CTA (and its TMEM) per SM
+constexpr int GC_MIN_UNIT = 512;          // complex values per work unit at least (16 stages)
 
 // byte offset of (row r, k-quad q) in a K-major operand tile of QPR quads per row: core
 // matrices of 8 rows x 16 B, K-adjacent core matrices 128 B apart, 8-row groups QPR*128 B
@@ -515,7 +516,9 @@ GcPlan gc_plan(int ma, int mb, long long K, int units) {
   const long long tiles = (long long)p.nit * p.njt;
   const long long sms = ef::sm_count();
   long long nk = (units * sms + tiles - 1) / tiles;           // about `units` units per SM
-  const long long maxk = (K + 2047) / 2048;                   // >= 2048 complex per unit
+  // >= GC_MIN_UNIT complex per unit: at small K (grids of 32^3-64^3) the units, not the
+  // SMs, would otherwise run out (2048 per unit left 32 of 152 SMs busy at 32^3)
+  const long long maxk = (K + GC_MIN_UNIT - 1) / GC_MIN_UNIT;
   if (nk > maxk) nk = maxk;
   if (nk < 1) nk = 1;
   long long kchunk = (K + nk - 1) / nk;

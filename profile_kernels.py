@@ -8,6 +8,12 @@
     python profile_kernels.py kpm --grid 256 --m 4 --steps 8
     python profile_kernels.py rowstats --ma 32 --mb 32 --grid 128
     python profile_kernels.py rownorms --ma 64 --grid 128
+    python profile_kernels.py batched --seeds 16
+
+`batched` runs the 48-instance grouped LOBPCG workload of bench.py (N in 64/216/512 x
+--seeds seeds on 32^3/48^3/64^3) twice untimed, once timed, and once under
+torch.profiler (CUPTI kernel records, not ncu), and prints the device time per kernel
+against the wall time.
 
 Each runs 3 warm-up calls and then --reps timed calls (default 1; CUDA events on
 the current stream), printing the mean time; under ncu, skip the warm-up launches
@@ -46,17 +52,71 @@ def _timed(fn, warm: int = 3) -> float:
     return s.elapsed_time(e) / REPS
 
 
+def _batched(seeds: int) -> None:
+    import collections
+    import time
+
+    from torch.profiler import ProfilerActivity, profile
+
+    import bench
+    from eigenfns_gb300.batched import lobpcg_batched
+    from eigenfns_gb300.operator import MaxwellOperator
+    from eigenfns_gb300.solver import lobpcg_blocks
+    from eigenfns_gb300.structure import bz_kpoint, make_structure
+    dev = torch.device("cuda", torch.cuda.current_device())
+    inst = []
+    for nodes, grid, nev, m, guard in bench.BATCHED_KINDS:
+        for j in range(seeds):
+            seed = 1000 * nodes + j
+            eps, L, _ = make_structure(nodes, grid, seed=seed)
+            inst.append((MaxwellOperator(eps, L, k_frac=bz_kpoint(seed), device=dev), nev, m, guard, seed))
+    for k in range(len(bench.BATCHED_KINDS)):
+        op, nev, m, g, s = inst[k * seeds]
+        lobpcg_blocks(op, nev, m=m, guard=g, tol=1e-4, seed=s, verbose=False)
+
+    def run():
+        return lobpcg_batched([i[0] for i in inst], [i[1] for i in inst], m=[i[2] for i in inst],
+                              guard=[i[3] for i in inst], tol=1e-4, seeds=[i[4] for i in inst])
+    run()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    run()
+    torch.cuda.synchronize()
+    print(f"batched wall {time.perf_counter() - t0:.3f} s")
+    with profile(activities=[ProfilerActivity.CPU, ProfilerActivity.CUDA]) as prof:
+        t0 = time.perf_counter()
+        run()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    agg = collections.defaultdict(lambda: [0, 0.0])
+    for e in prof.events():
+        if e.device_type == torch.autograd.DeviceType.CUDA:
+            a = agg[e.name[:90]]
+            a[0] += 1
+            a[1] += e.device_time_total
+    tot = sum(v[1] for v in agg.values())
+    print(f"profiled wall {wall * 1e3:.1f} ms, kernels {tot / 1e3:.1f} ms, "
+          f"launches {sum(v[0] for v in agg.values())}")
+    for k, v in sorted(agg.items(), key=lambda x: -x[1][1])[:30]:
+        print(f"{v[1] / 1e3:9.1f} ms {v[0]:7d} {v[1] / max(v[0], 1):8.1f} us  {k}")
+    print(prof.key_averages().table(sort_by="self_cpu_time_total", row_limit=12))
+
+
 def main(argv=None) -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("kernel", choices=["theta", "precond", "gram", "gram_tc", "rotate", "cheb", "kpm",
-                                       "rowstats", "rownorms", "residual"])
+                                       "rowstats", "rownorms", "residual", "batched"])
     ap.add_argument("--grid", type=int, default=128)
     ap.add_argument("--m", type=int, default=2)
     ap.add_argument("--ma", type=int, default=32)
     ap.add_argument("--mb", type=int, default=32)
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--reps", type=int, default=1, help="timed calls (mean reported)")
+    ap.add_argument("--seeds", type=int, default=16, help="batched: seeds per node count")
     a = ap.parse_args(argv)
+    if a.kernel == "batched":
+        _batched(a.seeds)
+        return
     global REPS
     REPS = max(1, a.reps)
     g = torch.Generator(device="cuda").manual_seed(1)
