@@ -28,7 +28,7 @@ import torch
 
 from . import blas, hosteig
 from .grouped import GroupResults
-from .solver import HostEigh, HostMany, lobpcg_steps
+from .solver import HostCopy, HostEigh, HostMany, lobpcg_steps
 
 
 class _EighOnHost:
@@ -49,7 +49,7 @@ def _request_to_host(req):
     if isinstance(req, HostMany):
         return [_request_to_host(r) for r in req.items]
     if isinstance(req, HostEigh):
-        return _EighOnHost(_pinned_copy(req.A))
+        return _EighOnHost(req.A.host if isinstance(req.A, HostCopy) else _pinned_copy(req.A))
     if isinstance(req, tuple):
         return tuple(_pinned_copy(t) for t in req)
     return _pinned_copy(req)

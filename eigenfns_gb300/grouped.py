@@ -29,7 +29,8 @@ import torch
 
 from . import blas, dense
 from ._lib import EF_RAND_NORMAL, call, load
-from .solver import (_RR_DEAD_PENALTY, _SVQB_DROP, HostEigh, HostMany, SolveStats, _ritz_from_host,
+from .solver import (_RR_DEAD_PENALTY, _SVQB_DROP, HostCopy, HostEigh, HostMany, SolveStats,
+                     _ritz_from_host,
                      svqb_from_eig)
 
 
@@ -306,13 +307,20 @@ def lobpcg_group_steps(ops, nevs, keys=None, m: int = 32, guard: int = 8, tol: f
             if not active:
                 break
             yield from ortho_steps(active, W, first=(ww[keep], Vw[keep]))
+
+            def theta_w():
+                st.theta(active, W, HW, m)
+                for i in active:
+                    stats[i].theta_applications += m
             with_p = [i for i in active if have_p[i]]
             if with_p:
                 XW = S[:, m:3 * m]
                 for _ in range(2):
                     Cm = st.gram(with_p, XW, P, 2 * m, m).to(torch.complex64)
                     st.rotate(with_p, Cm, XW, P, 2 * m, m, -1)
-                w, V = yield HostEigh(_hermitian(st.gram(with_p, P, P, m, m)[idx_t(with_p)]))
+                Gp = HostCopy(_hermitian(st.gram(with_p, P, P, m, m)[idx_t(with_p)]))
+                theta_w()                              # runs while the host does P's eigh
+                w, V = yield HostEigh(Gp)
                 keep_rows, Ts = [], []
                 for j, i in enumerate(with_p):
                     Tp, keepp = svqb_from_eig(w[j], V[j], _SVQB_DROP)
@@ -323,9 +331,8 @@ def lobpcg_group_steps(ops, nevs, keys=None, m: int = 32, guard: int = 8, tol: f
                         Ts.append(Tp.astype(np.complex64))
                 if keep_rows:
                     rotate_inplace(keep_rows, st.upload(keep_rows, np.stack(Ts), (m, m)), P, m)
-            st.theta(active, W, HW, m)
-            for i in active:
-                stats[i].theta_applications += m
+            else:
+                theta_w()
             with_p = [i for i in active if have_p[i]]
             if with_p:
                 st.theta(with_p, P, HP, m)

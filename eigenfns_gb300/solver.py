@@ -70,6 +70,24 @@ class HostEigh:
         self.A = A
 
 
+class HostCopy:
+    """A device tensor's copy into pinned host memory, queued when this is made, with an
+    event behind it. A step generator that yields HostEigh(HostCopy(A)) can queue more
+    device work between the two; the driver waits for this copy only, not for that
+    work, so the device runs it while the host computes the eigendecomposition."""
+    __slots__ = ("host", "event")
+
+    def __init__(self, t: torch.Tensor):
+        self.host = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+        self.host.copy_(t, non_blocking=True)
+        self.event = torch.cuda.Event()
+        self.event.record()
+
+    def numpy(self) -> np.ndarray:
+        self.event.synchronize()
+        return self.host.numpy()
+
+
 class HostMany:
     """A step generator's request for several host reads at once: a list of device
     tensors and HostEigh requests; the driver sends back the list of their results."""
@@ -158,7 +176,7 @@ def _to_host(req):
         return [_to_host(r) for r in req.items]
     if isinstance(req, HostEigh):
         from . import hosteig
-        A = req.A.cpu().numpy()
+        A = req.A.numpy() if isinstance(req.A, HostCopy) else req.A.cpu().numpy()
         return hosteig.eigh_many(A) if A.ndim == 3 else hosteig.eigh(A)
     if isinstance(req, tuple):
         return tuple(t.cpu().numpy() for t in req)
@@ -321,14 +339,19 @@ def lobpcg_steps(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
                 XW = S[m:3 * m]
                 for _ in range(2):
                     rotate(gram(XW, P).to(torch.complex64), XW, P, -1)
-                Tp, keepp = svqb_from_eig(*(yield HostEigh(_hermitian(gram(P, P)))))
+                Gp = HostCopy(_hermitian(gram(P, P)))
+                # Θ W depends on W alone: queued behind the copy of P's Gram, it runs on
+                # the device while the host does P's eigh
+                _theta(op, W, stats, out=HW)
+                Tp, keepp = svqb_from_eig(*(yield HostEigh(Gp)))
                 if not keepp.any():
                     have_p = False
                 elif m <= 32:
                     rotate(Tp.astype(np.complex64), P, P)
                 else:
                     P.copy_(rotate(Tp.astype(np.complex64), P))
-            _theta(op, W, stats, out=HW)
+            else:
+                _theta(op, W, stats, out=HW)
             if have_p:
                 _theta(op, P, stats, out=HP)
                 act, hact, off = S, HS, 0
