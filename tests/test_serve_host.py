@@ -164,3 +164,22 @@ def test_waiting_requests_start_as_groups(fake_server):
     res = srv.run(reqs, realtime=False)
     # one group per (grid, block) shape: 32^3 x {8, 16} and 48^3 x {8, 16}
     assert len(res) == 10 and srv.groups == 4 and srv.peak_concurrent == 10
+
+
+def test_full_shape_request_stream():
+    """bench_serve.py's stream: seeded, N paired with its grid (N = 1000 on 96^3 or 128^3),
+    8-120 bands, increasing arrivals, and every request fits the 160 GB admission budget."""
+    import sys
+    from pathlib import Path
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+    import bench_serve
+    from eigenfns_gb300 import serve
+    a = bench_serve.requests(64, seed=3, rate_hz=2.0, tol=1e-4)
+    b = bench_serve.requests(64, seed=3, rate_hz=2.0, tol=1e-4)
+    assert [(r.nodes, r.grid, r.nev, r.k_frac, r.arrival) for r in a] == \
+           [(r.nodes, r.grid, r.nev, r.k_frac, r.arrival) for r in b]
+    assert all((r.nodes, r.grid) in bench_serve.KINDS for r in a)
+    assert {r.grid for r in a} == {32, 48, 64, 96, 128}
+    assert all(8 <= r.nev <= 120 and r.tol == 1e-4 for r in a)
+    assert all(a[i].arrival < a[i + 1].arrival for i in range(63))
+    assert max(serve.footprint_bytes(r) for r in a) < 160e9
