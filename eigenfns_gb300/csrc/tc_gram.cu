@@ -66,6 +66,15 @@ constexpr int GC_RAW_MAX = 12;        // raw box stages at most (the rest of sha
 constexpr int GC_SEG = 4;             // stages per TMEM accumulation segment (32 k-steps)
 constexpr int GC_SMEM_MIN = 120 * 1024;   // keeps one CTA (and its TMEM) per SM
 constexpr int GC_MIN_UNIT = 512;          // complex values per work unit at least (16 stages)
+// TMEM split between accumulators and the operand ring (compile-time tuning knobs): at
+// most EF_GC_NACC_MAX accumulators (1 gives their columns to the operand ring) and at
+// most EF_GC_NBUF_MAX operand stages
+#ifndef EF_GC_NACC_MAX
+#define EF_GC_NACC_MAX 2
+#endif
+#ifndef EF_GC_NBUF_MAX
+#define EF_GC_NBUF_MAX 4
+#endif
 
 // byte offset of (row r, k-quad q) in a K-major operand tile of QPR quads per row: core
 // matrices of 8 rows x 16 B, K-adjacent core matrices 128 B apart, 8-row groups QPR*128 B
@@ -98,7 +107,7 @@ struct GcCfg {
   static constexpr int QPR = GC_KB / 4 / PK;                   // B quads per operand row
   static constexpr int ACOLS = 2 * GC_KB / PK;                 // TMEM columns of one A stage (hi, lo)
   static constexpr int DCOLS = 2 * NB * PK;                    // columns of one accumulator
-  static constexpr int NACC = 2 * DCOLS + 2 * ACOLS <= 512 ? 2 : 1;
+  static constexpr int NACC = (2 * DCOLS + 2 * ACOLS <= 512 && EF_GC_NACC_MAX >= 2) ? 2 : 1;
   static constexpr int MTMAX = 64 / PK;                        // A rows per box
   static constexpr int B_BYTES = 2 * NB * GC_KB * 4;           // [B_hi; B_lo] per stage
   // raw stage: A boxes for reals [0,32) and [32,64), then the two B boxes
@@ -107,7 +116,9 @@ struct GcCfg {
   // stages beside them in 226 KB of shared memory); the raw ring takes the rest of the
   // shared memory, which sets the bytes in flight from HBM
   static constexpr int SMEM_BUDGET = 226 * 1024 - 1024;
-  static constexpr int NBUF_TMEM = (512 - NACC * DCOLS) / ACOLS < 4 ? (512 - NACC * DCOLS) / ACOLS : 4;
+  static constexpr int NBUF_TMEM = (512 - NACC * DCOLS) / ACOLS < EF_GC_NBUF_MAX
+                                       ? (512 - NACC * DCOLS) / ACOLS
+                                       : EF_GC_NBUF_MAX;
   static constexpr int NBUF_SMEM = (SMEM_BUDGET - 4 * RAW_BYTES) / B_BYTES;
   static constexpr int NBUF = NBUF_TMEM < NBUF_SMEM ? NBUF_TMEM : NBUF_SMEM;
   static constexpr int NRAW = (SMEM_BUDGET - NBUF * B_BYTES) / RAW_BYTES < GC_RAW_MAX
