@@ -126,8 +126,9 @@ def gram(A: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
     return out
 
 
-def gram_tc(A: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
-    """gram() on the tcgen05 tensor cores (3xTF32 split, TMEM accumulators)."""
+def gram_tc(A: torch.Tensor, B: torch.Tensor) -> tuple:
+    """gram() on the tcgen05 tensor cores (3xTF32 split, TMEM accumulators): (G, err),
+    err a one-int device flag that a timed-out pipeline wait sets."""
     A, B = _c64(A), _c64(B)
     ma, K = _rows(A)
     mb, Kb = _rows(B)
