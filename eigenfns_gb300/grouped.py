@@ -155,6 +155,9 @@ def lobpcg_group_steps(ops, nevs, keys=None, m: int = 32, guard: int = 8, tol: f
     nevs = [int(v) for v in per(nevs)]
     seeds = [int(s) for s in per(0 if seeds is None else seeds)]
     keys = list(range(B)) if keys is None else list(keys)
+    from . import tune
+    for op in ops:                      # the pipeline a solve alone would use (solver.lobpcg_steps)
+        tune.apply_cached(op, m)
     st = _Stack(ops, dev)
     vshape = ops[0].vec_shape(1)[1:]
     nl = m - guard

@@ -256,7 +256,9 @@ def lobpcg_steps(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
 
     `autotune` (default: on when EF_AUTOTUNE=1) times the operator pipeline and the
     Gram schedules of this block size once on the running GPU before the solve and
-    reuses the cached choice afterwards (eigenfns_gb300.tune).
+    reuses the cached choice afterwards (eigenfns_gb300.tune). Left at None without
+    EF_AUTOTUNE, a pipeline stored by an earlier tuning of this grid edge and block
+    size is applied without timing; False leaves the operator as it is.
 
     Working set: two (3m, 2, G, G, G) slabs holding the blocks as [P; X; W] (the
     Rayleigh-Ritz basis is contiguous, so its Gram is one call and the Ritz
@@ -269,6 +271,8 @@ def lobpcg_steps(op, nev: int, m: int = 96, guard: int = 48, tol: float = 1e-4,
     from . import tune
     if tune.enabled(autotune) and hasattr(op, "configure"):
         tune.autotune(op, m)
+    elif autotune is None:
+        tune.apply_cached(op, m)        # a pipeline chosen earlier on this GPU, if any
     vshape = op.vec_shape(1)[1:]
     cap = int(np.ceil(nev / max(m - guard, 1))) * (m - guard) + m
     n_init = 0 if initial_locked is None else int(initial_locked.shape[0])

@@ -13,6 +13,9 @@ Each candidate runs `warmup` untimed calls and then `reps` timed calls (CUDA eve
 the current stream); the lowest mean wins. Choices are stored in a JSON file keyed by
 the GPU name, the library version and the shape ($EIGENFNS_GB300_TUNE_CACHE, else
 ~/.cache/eigenfns_gb300/tune.json), and later processes re-apply them without timing.
+The solvers (single and grouped LOBPCG) apply a stored operator choice to their
+operators by default (apply_cached), so an operator built after a tuning run gets the
+tuned pipeline; autotune=False leaves operators as they are.
 The choice of units does not change the Gram's arithmetic; the kernel choice selects
 between the mixed-precision (3xTF32) and the plain fp32 Gram, both fp32-class.
 """
@@ -107,6 +110,19 @@ def tune_operator(op, m: int, warmup: int = 2, reps: int = 3, use_cache: bool = 
            "candidates": [[p, b, t] for t, p, b in timings]}
     _store(key, res)
     return dict(res, cached=False)
+
+
+def apply_cached(op, m: int) -> bool:
+    """Apply the operator pipeline an earlier tuning chose for this GPU, grid edge and
+    block size, without timing anything; False (the operator left as it is) when the
+    cache holds no choice for it."""
+    if not hasattr(op, "configure"):
+        return False
+    hit = _load_cache().get(f"{_prefix(op.device)}|op|G={op.grid_size}|m={m}")
+    if hit is None:
+        return False
+    op.configure(hit["passes"], hit["subbatch_bytes"])
+    return True
 
 
 def apply_gram(ma: int, mb: int, kernel: int, units: int) -> None:
