@@ -116,8 +116,15 @@ class EigenServer:
     grouped solve; the running groups advance in one pipelined batch."""
 
     def __init__(self, budget_bytes: float = 160e9, max_concurrent: int = 16, device=None,
-                 group_wait: float = 0.5, min_group: int = 12, max_group: int = 32):
+                 group_wait: float = 0.5, min_group: int = 12, max_group: int = 32,
+                 exclusive_grid: int = 96):
+        """`exclusive_grid`: requests on grids of this edge or larger keep the device busy
+        alone (their kernels fill every SM), so interleaving two of them gains nothing
+        and lengthens both latencies: at most one such request runs at a time, by
+        itself, and lighter requests are admitted around it (a large request waiting
+        for the running one does not hold back the lighter requests behind it)."""
         self.budget = float(budget_bytes)
+        self.exclusive_grid = int(exclusive_grid)
         self.max_concurrent = int(max_concurrent)
         self.group_wait = float(group_wait)
         self.min_group = int(min_group)
@@ -172,16 +179,22 @@ class EigenServer:
         def admit(now):
             """Take arrived requests that fit (slots, memory) and start them as groups."""
             take = []
-            while pending:
-                head = pending[0]
-                fp = footprint_bytes(head)
-                arrived = (not realtime) or head.arrival <= now
-                if not (arrived and len(running) + len(take) < self.max_concurrent
-                        and self._used + fp <= self.budget):
+            heavy_busy = any(self._heavy(v[0]) for v in running.values())
+            i = 0
+            while i < len(pending):
+                head = pending[i]
+                if realtime and head.arrival > now:
                     break
-                pending.pop(0)
+                if self._heavy(head) and heavy_busy:
+                    i += 1                    # waits for the running large solve
+                    continue
+                fp = footprint_bytes(head)
+                if not (len(running) + len(take) < self.max_concurrent and self._used + fp <= self.budget):
+                    break
+                pending.pop(i)
                 self._used += fp
                 take.append((head, fp))
+                heavy_busy = heavy_busy or self._heavy(head)
             by_shape: dict = {}
             for req, fp in take:
                 by_shape.setdefault(_shape(req), []).append((req, fp))
@@ -203,7 +216,13 @@ class EigenServer:
         with torch.cuda.device(self.device):
             while pending or len(batch):
                 now = time.perf_counter() - t0
-                waiting = [r for r in pending[:self.min_group] if (not realtime) or r.arrival <= now]
+                heavy_busy = any(self._heavy(v[0]) for v in running.values())
+                waiting = []                  # arrived requests that could start now
+                for r in pending:
+                    if len(waiting) >= self.min_group or (realtime and r.arrival > now):
+                        break
+                    if not (heavy_busy and self._heavy(r)):
+                        waiting.append(r)
                 if waiting and (not running or len(waiting) >= self.min_group
                                 or now - waiting[0].arrival >= self.group_wait):
                     admit(now)
@@ -216,6 +235,10 @@ class EigenServer:
         if self.errors:
             raise RuntimeError(f"{len(self.errors)} request(s) failed: {self.errors[:3]}")
         return sorted(results, key=lambda r: r.rid)
+
+
+    def _heavy(self, req: SolveRequest) -> bool:
+        return req.grid >= self.exclusive_grid
 
 
 def run_plain(requests, device=None) -> list:

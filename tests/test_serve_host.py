@@ -183,3 +183,24 @@ def test_full_shape_request_stream():
     assert all(8 <= r.nev <= 120 and r.tol == 1e-4 for r in a)
     assert all(a[i].arrival < a[i + 1].arrival for i in range(63))
     assert max(serve.footprint_bytes(r) for r in a) < 160e9
+
+
+def test_large_grid_requests_run_alone_without_blocking_small_ones(fake_server):
+    """Requests on grids >= exclusive_grid run one at a time and by themselves; lighter
+    requests behind a waiting large one are admitted while it waits."""
+    serve, state = fake_server
+    big = [serve.SolveRequest(rid=i, nodes=1000, grid=128, seed=10 + i, nev=20, arrival=0.0)
+           for i in range(3)]
+    small = [serve.SolveRequest(rid=3 + i, nodes=64, grid=32, seed=20 + i, nev=9, arrival=0.001)
+             for i in range(4)]
+    srv = serve.EigenServer(budget_bytes=1e15, max_concurrent=16, device="cpu", group_wait=0.0,
+                            min_group=1)
+    res = {r.rid: r for r in srv.run(big + small, realtime=True)}
+    assert len(res) == 7
+    spans = sorted((res[i].start, res[i].end) for i in range(3))
+    assert all(spans[j][1] <= spans[j + 1][0] + 1e-6 for j in range(2))   # one at a time
+    assert all(res[3 + i].start < spans[1][0] for i in range(4))            # not held back
+    srv = serve.EigenServer(budget_bytes=1e15, max_concurrent=16, device="cpu", group_wait=0.0,
+                            min_group=1, exclusive_grid=1 << 30)
+    res = srv.run(big, realtime=False)
+    assert len({r.start for r in res}) == 1                                  # one group otherwise
