@@ -16,9 +16,9 @@ chebsi  Two-stage bandpass ChebSI at 192^3 with m = 104: build degree 3000 x 2
         outers, polish degree 12000 x up to 4 outers, stopping when every in-window
         pair converged (scripts/run_interior.py:154-216). The reference's window
         [1.757, 1.930] is in its own units (µm^-2 for its structures), so the window
-        here keeps its relative width (λ_hi/λ_lo = 1.098) and is placed where this
-        structure's KPM counting function (a 192^3 estimate, 8 probes, degree 2000)
-        gives about 69 modes inside, the size of the reference's S_below window.
+        here keeps its relative width (λ_hi/λ_lo = 1.098) and is placed at the lowest
+        λ where this structure's KPM counting function (a 192^3 estimate, 8 probes,
+        degree 6000) gives 69 modes inside, the size of the reference's S_below window.
 
 Each run prints one JSON line with its measurements.
 """
@@ -75,16 +75,28 @@ def run_kpm(a) -> dict:
             "counting": {"lam": lams.tolist(), "N": mean.tolist(), "se": se.tolist()}}
 
 
-def choose_window(op, lam_max: float, target: int = 69, probes: int = 8, degree: int = 2000):
-    """(λ_lo, λ_hi) with λ_hi = 1.098 λ_lo and about `target` modes inside (KPM count)."""
+def pick_window(lo: np.ndarray, n_lo: np.ndarray, n_hi: np.ndarray, target: int):
+    """Index of the lowest window [lo, lo * 1.098] whose estimated mode count reaches
+    `target` (the count grows with λ, roughly as λ^1.5), else of the largest count."""
+    inside = np.asarray(n_hi) - np.asarray(n_lo)
+    hit = np.nonzero(inside >= target)[0]
+    return int(hit[0]) if hit.size else int(np.argmax(inside))
+
+
+def choose_window(op, lam_max: float, target: int = 69, probes: int = 8, degree: int = 6000):
+    """(λ_lo, λ_hi) with λ_hi = 1.098 λ_lo and about `target` modes inside (KPM count).
+
+    The window sits at the bottom of the spectrum (at 192^3 a few hundred modes lie
+    below it, about 2e-4 of λ_max), so λ_lo is searched on a log scale from 1e-5 λ_max
+    and the moments go to degree 6000, whose Jackson resolution there (about a third of
+    the window's width) separates the window from its neighbourhood."""
     from eigenfns_gb300 import kpm
     mom = kpm.kpm_moments(op, lam_max, degree, probes, seed=11, probe_kind="complex")
-    lo = np.linspace(0.005, 0.5, 400) * lam_max
+    lo = np.geomspace(1e-5, 0.05, 800) * lam_max
     n_lo, _, _ = kpm.counting(mom, lam_max, lo)
     n_hi, _, _ = kpm.counting(mom, lam_max, lo * WINDOW_RATIO)
-    inside = n_hi - n_lo
-    j = int(np.argmin(np.abs(inside - target)))
-    return float(lo[j]), float(lo[j] * WINDOW_RATIO), float(inside[j]), float(n_lo[j])
+    j = pick_window(lo, n_lo, n_hi, target)
+    return float(lo[j]), float(lo[j] * WINDOW_RATIO), float(n_hi[j] - n_lo[j]), float(n_lo[j])
 
 
 def run_chebsi(a) -> dict:

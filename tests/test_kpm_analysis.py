@@ -68,3 +68,18 @@ def test_jackson_damping_properties():
     lam = (x + 1) * 5.0
     far = np.abs(lam - 3.0) > 0.3
     assert np.allclose(vals[far], (lam[far] < 3.0).astype(float), atol=2e-3)
+
+
+def test_interior_window_is_the_lowest_with_the_target_count():
+    """bench_interior.pick_window: the first window on the λ grid whose estimated count
+    reaches the target, for a count growing like λ^1.5 (the photonic band DOS)."""
+    import sys
+    from pathlib import Path
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+    import bench_interior as bi
+    lo = np.geomspace(1e-3, 10.0, 500)
+    count = lambda lam: 300.0 * lam ** 1.5
+    j = bi.pick_window(lo, count(lo), count(lo * bi.WINDOW_RATIO), 69)
+    inside = count(lo * bi.WINDOW_RATIO) - count(lo)
+    assert inside[j] >= 69 and (j == 0 or inside[j - 1] < 69)
+    assert bi.pick_window(lo, count(lo), count(lo * bi.WINDOW_RATIO), 10 ** 9) == len(lo) - 1
