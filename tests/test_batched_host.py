@@ -140,3 +140,25 @@ def test_combined_host_reads_and_stacked_eigh():
     assert np.array_equal(w[1], w1) and np.array_equal(V[1], V1)
     for i in range(3):
         assert np.allclose(A[i] @ V[i], V[i] * w[i][None, :], atol=1e-10)
+
+
+def test_host_copy_requests_are_read_without_a_second_copy():
+    """A HostEigh of a HostCopy (the copy queued before more device work) reaches the
+    eigendecomposition from its own pinned buffer, after its own event, in both drivers."""
+    import numpy as np
+    from eigenfns_gb300 import batched, solver
+
+    class _Event:
+        def __init__(self):
+            self.waited = False
+
+        def synchronize(self):
+            self.waited = True
+
+    hc = solver.HostCopy.__new__(solver.HostCopy)
+    hc.host = torch.diag(torch.tensor([3.0, 1.0, 2.0], dtype=torch.float64)).to(torch.complex128)
+    hc.event = _Event()
+    req = solver.HostEigh(hc)
+    assert batched._request_to_host(req).A is hc.host
+    w, V = solver._to_host(req)
+    assert hc.event.waited and np.allclose(w, [1.0, 2.0, 3.0]) and V.shape == (3, 3)
